@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Benchmark of the exact miniBUDE energy kernel on one GB300 (or N independent replicas).
+
+Workload: the scaled-up plain-kernel deck -- 4,096 protein atoms (+-30 A box), 64 ligand atoms,
+34 forcefield types, 1,048,576 poses -- generated from a seed in the reference's deck layout.
+A step is one evaluation of every pose (pose transforms + exact kernel).
+
+Printed (one JSON line, rank 0):
+  value      exact GInteractions/s = nposes*natlig*natpro / step time, inputs resident in HBM, CUDA
+             events on the library's stream, L2 flushed (512 MB memset) before every timed step
+  e2e        the same metric through the C-ABI from pinned host buffers: per step the poses and
+             ligand go host->device, the energies come back device->host
+  roofline   the exact kernel against the FP32 peak (SMs x 128 lanes x 2 x clock), using the
+             reference's own operation count (30 per interaction + 18 per pose and ligand atom +
+             28 per pose, src/main.cpp:359)
+  cpu_baseline  the oracle's FP32 restatement of the reference kernel (OpenMP, -O3 -ffast-math as
+             the reference's release build) on a bounded sample of the same deck, all host cores
+
+`--impl reference` times that CPU implementation alone, as the reference arm.
+Under torchrun each rank runs its own deck (seed = rank) on its own GPU: weak scaling, no
+data-path collective; a gloo barrier and a max-reduce of the step time are the only exchange.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from minibude_gb300 import LARGE, SMALL, synthetic_deck  # noqa: E402
+from minibude_gb300.validate import algorithmic_flops  # noqa: E402
+
+METRIC = "exact GInteractions/s"
+UNIT = "GInteractions/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["large", "small"], default="large")
+    ap.add_argument("--cfg", default="auto", help="auto, or ppwi,wgsize,split,tile")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+class Dist:
+    """Rank bookkeeping; torch.distributed (gloo) only for the barrier and the max-reduce."""
+
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, sm_max_default: float):
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": sm_max_default, "reasons": ["unsampled"], "samples": 0}
+
+        def num(s):
+            try:
+                return float(s)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else sm_max_default,
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+def traffic_per_launch(nposes: int):
+    """DRAM bytes per exact-kernel launch from the committed ncu summary (scaled to nposes)."""
+    path = os.path.join(ROOT, "profiles", "exact_kernel_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    vals = {}
+    for line in open(path):
+        if ":" in line and not line.startswith("#"):
+            k, v = line.split(":", 1)
+            vals[k.strip()] = v.strip()
+    try:
+        return float(vals["dram_bytes_per_pose"]) * nposes
+    except (KeyError, ValueError):
+        return None
+
+
+def cpu_sample_run(deck, seconds: float, fast: bool = True):
+    """Time the oracle on the first S poses of `deck`, S sized for about `seconds` of work."""
+    import oracle
+    nthreads = os.cpu_count() or 1
+    probe = deck.head(min(deck.nposes, 256))
+    t = time.perf_counter()
+    oracle.fasten_f32(probe, nthreads=nthreads, fast=fast)
+    dt = max(time.perf_counter() - t, 1e-4)
+    n = int(min(deck.nposes, max(256, probe.nposes * seconds / dt)))
+    n = max(256, n // 256 * 256)
+    sample = deck.head(n)
+    t = time.perf_counter()
+    oracle.fasten_f32(sample, nthreads=nthreads, fast=fast)
+    dt = time.perf_counter() - t
+    return {"value": sample.interactions / dt / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"first {n} of {deck.nposes} poses of the same deck ({sample.interactions:.3e} interactions, "
+                      f"{dt:.1f} s); oracle/bude_oracle.c built -O3 -ffast-math -fopenmp"}
+
+
+def parse_cfg(ctx, text: str, deck):
+    from minibude_gb300.model import launch_cfg
+    if text != "auto":
+        p, w, s, t = (int(x) for x in text.split(","))
+        return launch_cfg(p, w, s, t)
+    try:
+        from minibude_gb300 import tune
+        return tune.pick(ctx, deck)
+    except ImportError:
+        return ctx.default_cfg(8, 128)
+
+
+def run_ours(args, dist: Dist):
+    from minibude_gb300 import build
+    from minibude_gb300.model import GpuContext, PinnedBuffer
+    build.build_library()
+    spec = LARGE if args.workload == "large" else SMALL
+    deck = synthetic_deck(spec, seed=dist.rank)
+    peaks = measured_peaks()
+    ctx = GpuContext(dist.local_rank)
+    ctx.upload(deck)
+    cfg = parse_cfg(ctx, args.cfg, deck)
+    ctx.run_many(cfg, max(args.warmup, 1), flush_l2=True)
+    launches0 = ctx.launch_count()
+    with ClockSampler(dist.local_rank) as clocks:
+        dist.barrier()
+        ms, exact_ms = ctx.run_many(cfg, args.steps, flush_l2=True)
+        dist.barrier()
+    launches = ctx.launch_count() - launches0
+    clk = clocks.summary(peaks.get("sm_max_mhz", 2070.0))
+    step_ms = float(np.mean(ms))
+    step_ms_max = dist.max(step_ms)
+    interactions = deck.interactions
+    value = dist.world * interactions / (step_ms_max * 1e-3) / 1e9
+
+    # Roofline of the exact kernel (the dominant kernel: the transform kernel is ~0.01% of a step).
+    exact_s = float(np.mean(exact_ms)) * 1e-3
+    flops = algorithmic_flops(deck.nposes, deck.natlig, deck.natpro)
+    achieved = flops / exact_s / 1e12
+    sms = _sm_count(dist.local_rank)
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
+    roof = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
+            "frac": round(achieved / peak, 4),
+            "peak_source": f"{sms} SMs x 128 FP32 lanes x 2 x {sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json); "
+                           "no measured FP32 peak exists, so this is the nominal peak at the measured max clock",
+            "work": "30 FLOP/interaction + 18/(pose, ligand atom) + 28/pose (src/main.cpp:359)",
+            "kernel": "exact_kernel", "kernel_ms": round(exact_s * 1e3, 4),
+            "traffic": traffic_per_launch(deck.nposes)}
+    if clk.get("sm_mhz"):
+        roof["frac_at_sampled_clock"] = round(achieved / (sms * 128 * 2 * clk["sm_mhz"] * 1e6 / 1e12), 4)
+
+    out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(step_ms_max, 4), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded; deck layout of the reference, shapes/distributions of the 4096-atom workload)",
+           "config": {"workload": spec.name, "natpro": deck.natpro, "natlig": deck.natlig, "ntypes": deck.ntypes,
+                      "nposes": deck.nposes, "launch": cfg.as_dict(),
+                      "l2": "flushed before every timed step (512 MB memset)",
+                      "parallelism": f"replicas x{dist.world} (one deck per rank)"},
+           "gpu_launches": launches, "clocks": clk, "roofline": roof}
+
+    if not args.no_e2e:
+        # End to end through the C-ABI from pinned host buffers.
+        pin_p = PinnedBuffer((6, deck.nposes))
+        pin_p.array[...] = deck.poses
+        pin_e = PinnedBuffer((deck.nposes,))
+        for _ in range(max(args.warmup, 1)):
+            ctx.score_host(cfg, pin_p.array, pin_e.array, ligand=deck.ligand)
+        dist.barrier()
+        ts = []
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            ctx.score_host(cfg, pin_p.array, pin_e.array, ligand=deck.ligand)
+            ts.append(time.perf_counter() - t)
+        dist.barrier()
+        e2e_s = dist.max(float(np.mean(ts)))
+        out["e2e"] = {"value": round(dist.world * interactions / e2e_s / 1e9, 3), "unit": UNIT,
+                      "h2d_bytes_per_step": int(deck.poses.nbytes + deck.ligand.nbytes),
+                      "d2h_bytes_per_step": int(deck.nposes * 4), "ms_per_step": round(e2e_s * 1e3, 4)}
+        pin_p.free()
+        pin_e.free()
+    ctx.close()
+
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_sample_run(deck, args.cpu_seconds)
+    return out
+
+
+def _sm_count(device: int) -> int:
+    from minibude_gb300.model import sm_count
+    return sm_count(device)
+
+
+def run_reference(args, dist: Dist):
+    """The reference arm: the reference's CPU implementation of the path on the host cores."""
+    import oracle
+    spec = LARGE if args.workload == "large" else SMALL
+    deck = synthetic_deck(spec, seed=0)
+    nthreads = os.cpu_count() or 1
+    use_ref = oracle.reference_available()
+    # Each step evaluates a bounded sample of the deck, sized so the whole run stays short.
+    per_step = max(0.5, min(8.0, 150.0 / max(args.steps + args.warmup, 1)))
+    probe = deck.head(256)
+    t = time.perf_counter()
+    (oracle.ref_omp_fasten(probe, 16) if use_ref else oracle.fasten_f32(probe, nthreads=nthreads, fast=True))
+    dt = max(time.perf_counter() - t, 1e-4)
+    n = int(max(256, min(deck.nposes, probe.nposes * per_step / dt)) // 256 * 256)
+    sample = deck.head(n)
+    ts = []
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        if use_ref:
+            oracle.ref_omp_fasten(sample, 16)
+        else:
+            oracle.fasten_f32(sample, nthreads=nthreads, fast=True)
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - t)
+    step = float(np.mean(ts))
+    value = sample.interactions / step / 1e9
+    kind = "reference" if use_ref else "port"
+    what = ("the reference's OmpBude<16> built from its sources (oracle/_ref)" if use_ref else
+            "oracle/bude_oracle.c (restatement of src/serial/fasten.hpp:18-132, parallel like "
+            "src/omp/fasten.hpp:235-254) built -O3 -ffast-math -fopenmp")
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded; same deck as the GPU arm)",
+            "config": {"workload": spec.name, "natpro": deck.natpro, "natlig": deck.natlig, "ntypes": deck.ntypes,
+                       "nposes": deck.nposes, "sample_poses_per_step": n},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": nthreads, "kind": kind,
+                             "sample": f"first {n} poses per step; {what}"},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+
+
+def main():
+    args = parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            if dist.rank != 0:
+                return
+            out = run_reference(args, dist)
+        else:
+            out = run_ours(args, dist)
+        if dist.rank == 0:
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,139 @@
+/*
+ * minibude_gb300.h -- C-ABI of the GB300 (sm_103a) miniBUDE energy-evaluation library
+ * (libbude_gb300.so).
+ *
+ * Plain C types, integer status codes and caller-owned buffers only.  Every entry point is the
+ * replacement for one piece of the reference's CUDA model, src/cuda/fasten.hpp (the `CudaBude`
+ * class behind the `Bude<PPWI>` interface of src/bude.h:95-101); each declaration below names the
+ * reference lines it replaces.  The C++ `Bude<PPWI>` model in minibude_gb300/model/gb300/fasten.hpp
+ * and the Python host (minibude_gb300/__init__.py) are thin wrappers over these symbols.
+ *
+ * Threading: a context is used from one host thread at a time (the reference calls `fasten`
+ * sequentially from one thread, src/main.cpp:517-541).  Error text is per host thread.
+ */
+#ifndef MINIBUDE_GB300_H
+#define MINIBUDE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Record layouts of the deck files; byte-identical to the reference's packed structs
+ * `Atom` (src/bude.h:39-42) and `FFParams` (src/bude.h:44-49). */
+typedef struct bude_atom {
+  float x, y, z;
+  int32_t type; /* index into the forcefield table */
+} bude_atom;
+
+typedef struct bude_ffparams {
+  int32_t hbtype; /* ASCII code of the bhff electrostatic type: '-' 45, 'D' 68, 'E' 69, 'F' 70 */
+  float radius, hphb, elsc;
+} bude_ffparams;
+
+/* Status codes.  The C++ model turns any non-zero code into std::runtime_error with the text of
+ * bude_gpu_last_error(), as the reference's checkError does (src/cuda/fasten.hpp:168-172). */
+#define BUDE_OK 0
+#define BUDE_ERR_ARG (-1)     /* bad size, pointer or launch shape */
+#define BUDE_ERR_CUDA (-2)    /* a CUDA runtime call failed */
+#define BUDE_ERR_STATE (-3)   /* call out of order (e.g. run before upload) */
+#define BUDE_ERR_TIMEOUT (-4) /* a bounded device-side wait ran out; the kernel returned early */
+#define BUDE_ERR_TYPE (-5)    /* an atom type index lies outside the forcefield table */
+
+/* Kernel launch shape of the exact kernel.  The reference exposes two knobs, PPWI (poses per work
+ * item, a template parameter, src/main.cpp:48-53) and wgsize (threads per block,
+ * src/cuda/fasten.hpp:272-275); this kernel adds the protein split and the shared-memory tile. */
+typedef struct bude_launch_cfg {
+  int32_t ppwi;   /* poses per thread, held in registers: 1, 2, 4, 8 or 16 */
+  int32_t wgsize; /* threads per block: a multiple of 32 in [32, 512] */
+  int32_t split;  /* protein slices per pose block, reduced across a thread-block cluster: 1..8 */
+  int32_t tile;   /* protein atoms per shared-memory stage (TMA bulk copy): multiple of 8, 8..512 */
+} bude_launch_cfg;
+
+typedef struct bude_gpu_ctx bude_gpu_ctx;
+
+/* Text of the last error raised on this host thread ("" if none). */
+const char *bude_gpu_last_error(void);
+
+/* Library version string, e.g. "minibude-gb300 0.1 (sm_103a)". */
+const char *bude_gpu_version(void);
+
+/* Device enumeration; replaces CudaBude::enumerateDevices (src/cuda/fasten.hpp:181-196).
+ * The name has the reference's form "<name> (<MB>MB;sm_<cc>)". */
+int bude_gpu_device_count(int *count);
+int bude_gpu_device_name(int device, char *buf, size_t buflen);
+/* Streaming multiprocessors of the device (sizes launch grids and the FP32 peak). */
+int bude_gpu_sm_count(int device, int *sms);
+
+/* Architecture check; replaces CudaBude::compatible and its `version` probe kernel
+ * (src/cuda/fasten.hpp:12-18, 218-248).  Writes the compute capability the kernels were built
+ * for and the device's own (both as 10*major+minor) and sets *ok to 1 when they match. */
+int bude_gpu_compatible(int device, int *kernel_cc, int *device_cc, int *ok);
+
+/* Context: device selection and the library's stream (src/cuda/fasten.hpp:252). */
+int bude_gpu_create(int device, bude_gpu_ctx **out);
+/* Frees every device buffer of the context (src/cuda/fasten.hpp:291-301). */
+int bude_gpu_destroy(bude_gpu_ctx *ctx);
+
+/* Upload a deck: protein, ligand, forcefield and poses; replaces the "context" allocation and
+ * copies of src/cuda/fasten.hpp:256-270.  `poses` holds six float fields (tilt, roll, pan in
+ * radians; x, y, z translation) at poses + k*pose_stride, the layout of poses.in
+ * (src/main.cpp:296-311).  Atom types are checked against ntypes (BUDE_ERR_TYPE).  Buffers grow
+ * as needed and are reused by later uploads. */
+int bude_gpu_upload(bude_gpu_ctx *ctx, const bude_atom *protein, int32_t natpro, const bude_atom *ligand,
+                    int32_t natlig, const bude_ffparams *forcefield, int32_t ntypes, const float *poses,
+                    int64_t pose_stride, int64_t nposes);
+
+/* Replace only the poses (and, when ligand != NULL, the ligand) of an uploaded deck. */
+int bude_gpu_set_poses(bude_gpu_ctx *ctx, const bude_atom *ligand, int32_t natlig, const float *poses,
+                       int64_t pose_stride, int64_t nposes);
+
+/* Map the reference's (PPWI, wgsize) pair onto this kernel's launch shape, choosing split and tile
+ * for the uploaded deck.  PPWI above 16 uses 16 poses per thread; wgsize 0 or below 32 is rounded
+ * up to a multiple of 32.  Results do not depend on the shape beyond FP32 summation order. */
+int bude_gpu_default_cfg(const bude_gpu_ctx *ctx, int32_t ppwi, int32_t wgsize, bude_launch_cfg *cfg);
+
+/* One evaluation of all uploaded poses (one iteration of the reference's hot loop,
+ * src/cuda/fasten.hpp:277-286): pose transforms and the exact kernel on the context's stream,
+ * then a stream synchronise.  *kernel_ms (optional) receives the CUDA-event time of the two
+ * kernels.  Energies stay on the device. */
+int bude_gpu_run(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, float *kernel_ms);
+
+/* `iterations` back-to-back evaluations, each timed with CUDA events on the context's stream;
+ * with flush_l2 != 0 a buffer larger than L2 is rewritten before each timed evaluation (outside
+ * the timed span).  ms_per_iter (optional) receives the time of each evaluation (both kernels),
+ * exact_ms_per_iter (optional) that of the exact kernel alone. */
+int bude_gpu_run_many(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, int32_t iterations, int32_t flush_l2,
+                      float *ms_per_iter, float *exact_ms_per_iter);
+
+/* Copy the energies of the last evaluation to the host (src/cuda/fasten.hpp:288-289). */
+int bude_gpu_download(bude_gpu_ctx *ctx, float *energies, int64_t nposes);
+
+/* End-to-end evaluation from host buffers: copies `poses` (and the ligand, when not NULL) to the
+ * device, evaluates, and copies the energies back, all on the context's stream. */
+int bude_gpu_score_host(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, const bude_atom *ligand, int32_t natlig,
+                        const float *poses, int64_t pose_stride, int64_t nposes, float *energies);
+
+/* The whole of CudaBude<PPWI>::fasten (src/cuda/fasten.hpp:250-305) in one call: create a context
+ * on `device`, upload, run `iterations` times, download, destroy.  kernel_ms (optional) receives
+ * `iterations` per-iteration times, context_ms (optional) the upload time. */
+int bude_gpu_fasten(int device, int32_t ppwi, int32_t wgsize, const bude_atom *protein, int32_t natpro,
+                    const bude_atom *ligand, int32_t natlig, const bude_ffparams *forcefield, int32_t ntypes,
+                    const float *poses, int64_t pose_stride, int64_t nposes, int32_t iterations, float *energies,
+                    float *kernel_ms, float *context_ms);
+
+/* Number of kernels this library launched on the context since it was created (the transform
+ * and exact kernels count one each). */
+int bude_gpu_launch_count(const bude_gpu_ctx *ctx, int64_t *count);
+
+/* Page-locked host buffers for callers that time host<->device copies. */
+int bude_host_alloc(size_t bytes, void **ptr);
+int bude_host_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MINIBUDE_GB300_H */

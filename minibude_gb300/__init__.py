@@ -1,0 +1,15 @@
+"""minibude_gb300 -- GB300-native (sm_103a) implementation of miniBUDE's energy-evaluation hot path.
+
+The compute lives in libbude_gb300.so (CUDA kernels + the C-ABI of include/minibude_gb300.h).
+This package is the Python host side: deck files (`deck`), the reference's validation and
+statistics (`validate`), the ctypes binding (`capi`) and the reference-shaped model interface
+(`model`).
+"""
+from .deck import (ATOM_DTYPE, FF_DTYPE, LARGE, SMALL, SPECS, Deck, DeckSpec, read_deck, synthetic_deck,
+                   write_deck)
+from .validate import DIFF_TOLERANCE_PCT, evaluate, validate, validate_abs
+
+__all__ = [
+    "ATOM_DTYPE", "FF_DTYPE", "LARGE", "SMALL", "SPECS", "Deck", "DeckSpec", "read_deck", "synthetic_deck",
+    "write_deck", "DIFF_TOLERANCE_PCT", "evaluate", "validate", "validate_abs",
+]

@@ -1,0 +1,103 @@
+"""Build the native parts in-tree: libbude_gb300.so (nvcc, sm_103a) and the C++ driver.
+
+Used by ``__graft_entry__.build()`` and by ``python -m minibude_gb300.build``.  Outputs land next
+to the sources (git-ignored) so the library that runs is always the in-tree one.
+"""
+from __future__ import annotations
+
+import concurrent.futures
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libbude_gb300.so")
+DRIVER_BIN = os.path.join(PKG, "bin", "gb300-bude")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+# Translation units of libbude_gb300.so; each compiles in parallel.
+CU_SOURCES = ["bude_gb300.cu", "arch_probe.cu"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd, cwd=None):
+    r = subprocess.run(cmd, cwd=cwd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: " + " ".join(cmd) + "\n" + r.stdout)
+    return r.stdout
+
+
+def _stale(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _csrc_deps():
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+
+
+def build_library(force: bool = False, verbose: bool = False) -> str:
+    """Compile every .cu file for sm_103a and link libbude_gb300.so."""
+    os.makedirs(BUILD, exist_ok=True)
+    deps = _csrc_deps()
+    if not force and not _stale(LIB, deps):
+        return LIB
+    nv = nvcc()
+    objs = []
+    jobs = []
+    for src in CU_SOURCES:
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+        objs.append(obj)
+        cmd = [nv, *ARCH, *NVCC_FLAGS, "-Xptxas", "-v", "-c", os.path.join(CSRC, src), "-o", obj]
+        jobs.append(cmd)
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        outs = list(ex.map(_run, jobs))
+    if verbose:
+        for o in outs:
+            sys.stdout.write(o)
+    tmp = LIB + ".tmp"
+    _run([nv, *ARCH, "-shared", "-o", tmp, *objs])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_driver(force: bool = False) -> str:
+    """The C++ driver binary (gb300-bude): the reference's CLI/YAML contract over the C-ABI."""
+    src = os.path.join(PKG, "driver", "main.cpp")
+    if not os.path.exists(src):
+        return ""
+    deps = [src, LIB] + [os.path.join(PKG, "driver", f) for f in os.listdir(os.path.join(PKG, "driver"))]
+    deps += [os.path.join(PKG, "model", "gb300", f) for f in os.listdir(os.path.join(PKG, "model", "gb300"))]
+    if not force and not _stale(DRIVER_BIN, deps):
+        return DRIVER_BIN
+    os.makedirs(os.path.dirname(DRIVER_BIN), exist_ok=True)
+    cxx = os.environ.get("CXX", "g++")
+    _run([cxx, "-std=c++17", "-O2", "-Wall", f"-I{INCLUDE}", f"-I{os.path.join(PKG, 'driver')}",
+          f"-I{os.path.join(PKG, 'model')}", "-DGB300", src, "-o", DRIVER_BIN, f"-L{PKG}", "-lbude_gb300",
+          f"-Wl,-rpath,{PKG}"])
+    return DRIVER_BIN
+
+
+def build_all(force: bool = False, verbose: bool = False) -> None:
+    build_library(force=force, verbose=verbose)
+    build_driver(force=force)
+
+
+if __name__ == "__main__":
+    build_all(force="--force" in sys.argv, verbose=True)
+    print(LIB)

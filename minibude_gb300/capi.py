@@ -1,0 +1,120 @@
+"""ctypes binding of libbude_gb300.so (declarations in include/minibude_gb300.h).
+
+This module only describes the C-ABI; `minibude_gb300.model` builds the reference-shaped
+interface on top of it.  Loading fails loudly when the library is missing: there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+from . import build as _build
+
+c_int32 = ctypes.c_int32
+c_int64 = ctypes.c_int64
+c_float_p = ctypes.POINTER(ctypes.c_float)
+c_void_p = ctypes.c_void_p
+
+BUDE_OK = 0
+BUDE_ERR_ARG = -1
+BUDE_ERR_CUDA = -2
+BUDE_ERR_STATE = -3
+BUDE_ERR_TIMEOUT = -4
+BUDE_ERR_TYPE = -5
+
+STATUS_NAMES = {
+    BUDE_OK: "BUDE_OK", BUDE_ERR_ARG: "BUDE_ERR_ARG", BUDE_ERR_CUDA: "BUDE_ERR_CUDA",
+    BUDE_ERR_STATE: "BUDE_ERR_STATE", BUDE_ERR_TIMEOUT: "BUDE_ERR_TIMEOUT", BUDE_ERR_TYPE: "BUDE_ERR_TYPE",
+}
+
+
+class BudeLaunchCfg(ctypes.Structure):
+    _fields_ = [("ppwi", c_int32), ("wgsize", c_int32), ("split", c_int32), ("tile", c_int32)]
+
+    def as_dict(self):
+        return {"ppwi": self.ppwi, "wgsize": self.wgsize, "split": self.split, "tile": self.tile}
+
+    def __repr__(self):
+        return "BudeLaunchCfg(%s)" % ", ".join(f"{k}={v}" for k, v in self.as_dict().items())
+
+
+class BudeError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+# (name, restype, argtypes) of every exported symbol.
+_P = c_void_p
+SIGNATURES = [
+    ("bude_gpu_last_error", ctypes.c_char_p, []),
+    ("bude_gpu_version", ctypes.c_char_p, []),
+    ("bude_gpu_device_count", ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
+    ("bude_gpu_device_name", ctypes.c_int, [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]),
+    ("bude_gpu_sm_count", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    ("bude_gpu_compatible", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int)]),
+    ("bude_gpu_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(c_void_p)]),
+    ("bude_gpu_destroy", ctypes.c_int, [_P]),
+    ("bude_gpu_upload", ctypes.c_int, [_P, _P, c_int32, _P, c_int32, _P, c_int32, _P, c_int64, c_int64]),
+    ("bude_gpu_set_poses", ctypes.c_int, [_P, _P, c_int32, _P, c_int64, c_int64]),
+    ("bude_gpu_default_cfg", ctypes.c_int, [_P, c_int32, c_int32, ctypes.POINTER(BudeLaunchCfg)]),
+    ("bude_gpu_run", ctypes.c_int, [_P, ctypes.POINTER(BudeLaunchCfg), c_float_p]),
+    ("bude_gpu_run_many", ctypes.c_int, [_P, ctypes.POINTER(BudeLaunchCfg), c_int32, c_int32, c_float_p,
+                                         c_float_p]),
+    ("bude_gpu_download", ctypes.c_int, [_P, c_float_p, c_int64]),
+    ("bude_gpu_score_host", ctypes.c_int, [_P, ctypes.POINTER(BudeLaunchCfg), _P, c_int32, _P, c_int64, c_int64,
+                                           c_float_p]),
+    ("bude_gpu_fasten", ctypes.c_int, [ctypes.c_int, c_int32, c_int32, _P, c_int32, _P, c_int32, _P, c_int32, _P,
+                                       c_int64, c_int64, c_int32, c_float_p, c_float_p, c_float_p]),
+    ("bude_gpu_launch_count", ctypes.c_int, [_P, ctypes.POINTER(c_int64)]),
+    ("bude_host_alloc", ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
+    ("bude_host_free", ctypes.c_int, [c_void_p]),
+]
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded library (built on first use if the sources are newer)."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"libbude_gb300.so is missing ({path}); build it with "
+                               "`python -c 'import __graft_entry__ as g; g.build()'` -- there is no CPU fallback")
+        l = ctypes.CDLL(path)
+        for name, res, args in SIGNATURES:
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def last_error() -> str:
+    return lib().bude_gpu_last_error().decode()
+
+
+def check(code: int) -> None:
+    if code != BUDE_OK:
+        raise BudeError(code, last_error())
+
+
+def ptr(a) -> c_void_p:
+    """Data pointer of a numpy array (None stays NULL)."""
+    if a is None:
+        return None
+    return c_void_p(a.ctypes.data)
+
+
+def fptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(c_float_p)

@@ -1,0 +1,592 @@
+// bude_gb300.cu -- host side of libbude_gb300.so: the C-ABI declared in include/minibude_gb300.h.
+//
+// It owns what the reference's CudaBude owns (src/cuda/fasten.hpp:174-305): device selection,
+// device buffers for the deck, kernel launches, per-iteration timing and the copy back -- plus
+// the per-deck slab of protein records the exact kernel streams (see exact_kernel.cuh).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/minibude_gb300.h"
+#include "exact_kernel.cuh"
+#include "internal.h"
+
+namespace bude {
+
+// ---------------------------------------------------------------------------------------------
+// Errors
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char *what) {
+  return set_error(BUDE_ERR_CUDA, "%s: %s: %s", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+const char *last_error() { return g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------------------------
+// Pair constants (reference pair set-up, src/serial/fasten.hpp:80-96 and src/bude.h:22-35).
+// Each record feeds the three saturating FMAs of exact_kernel; the derived constants are evaluated
+// in double and rounded once, which is at least as close to the reference's FP32 expressions as
+// any FP32 evaluation order.
+void pair_record(const bude_ffparams &L, const bude_ffparams &Pp, float px, float py, float pz, float *rec) {
+  const float radij = Pp.radius + L.radius; // FP32 sum, as the reference
+  const bool both_f = Pp.hbtype == kHbtypeF && L.hbtype == kHbtypeF;
+  const double elcdst1 = both_f ? 0.25 : 0.5;
+  const bool type_e = Pp.hbtype == kHbtypeE || L.hbtype == kHbtypeE;
+  const bool p_ltz = Pp.hphb < 0.f, p_gtz = Pp.hphb > 0.f, p_nz = Pp.hphb != 0.f;
+  const bool l_ltz = L.hphb < 0.f, l_gtz = L.hphb > 0.f;
+  const float p_hphb = Pp.hphb * ((p_ltz && l_gtz) ? -1.f : 1.f);
+  const float l_hphb = L.hphb * ((p_gtz && l_ltz) ? -1.f : 1.f);
+  const float distdslv = p_ltz ? (l_ltz ? kNpNpDist : kNpPDist) : (l_ltz ? kNpPDist : -FLT_MAX);
+  const bool dslv_on = p_nz && distdslv > 0.f; // -FLT_MAX distance: the term can never fire
+  const double r_distdslv = dslv_on ? 1.0 / (double)distdslv : 1.0;
+  const float chrg_init = L.elsc * Pp.elsc;
+  const float dslv_init = p_hphb + l_hphb;
+  rec[0] = px;
+  rec[1] = py;
+  rec[2] = pz;
+  rec[3] = (float)(-1.0 / (double)radij);
+  rec[4] = (float)(-elcdst1);
+  rec[5] = (float)(1.0 + (double)radij * elcdst1);
+  rec[6] = (float)(-r_distdslv);
+  rec[7] = dslv_on ? (float)(1.0 + (double)radij * r_distdslv) : 0.f;
+  rec[8] = kCnstnt * (type_e ? -std::fabs(chrg_init) : chrg_init);
+  rec[9] = dslv_on ? dslv_init : 0.f;
+  rec[10] = 0.f;
+  rec[11] = 0.f;
+}
+
+// A padding atom: far away (every saturating factor is 0) with zero charge/desolvation weights.
+void null_record(float *rec) {
+  const float far = 1.0e15f;
+  rec[0] = rec[1] = rec[2] = far;
+  rec[3] = -1.f;
+  rec[4] = -1.f;
+  rec[5] = 0.f;
+  rec[6] = -1.f;
+  rec[7] = 0.f;
+  rec[8] = rec[9] = rec[10] = rec[11] = 0.f;
+}
+
+// slab[t][j] = record for ligand type t against protein atom j; rows padded to natpro_pad.
+void build_slab(const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes, int natpro_pad,
+                std::vector<float> &slab) {
+  slab.assign((size_t)ntypes * natpro_pad * 12, 0.f);
+  for (int t = 0; t < ntypes; ++t) {
+    float *row = slab.data() + (size_t)t * natpro_pad * 12;
+    for (int j = 0; j < natpro; ++j)
+      pair_record(ff[t], ff[protein[j].type], protein[j].x, protein[j].y, protein[j].z, row + (size_t)j * 12);
+    for (int j = natpro; j < natpro_pad; ++j) null_record(row + (size_t)j * 12);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Device buffers
+int DevBuf::reserve(size_t nbytes, const char *what) {
+  if (nbytes <= cap) return BUDE_OK;
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(nbytes, 256));
+  if (e != cudaSuccess) return cuda_error(e, what);
+  cap = nbytes;
+  return BUDE_OK;
+}
+
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+}
+
+} // namespace bude
+
+using namespace bude;
+
+struct bude_gpu_ctx : public bude::Context {};
+
+// ---------------------------------------------------------------------------------------------
+// Launch helpers
+
+namespace bude {
+
+static int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+static int ppwi_to_p(int ppwi) {
+  if (ppwi >= 16) return 16;
+  if (ppwi >= 8) return 8;
+  if (ppwi >= 4) return 4;
+  if (ppwi >= 2) return 2;
+  return 1;
+}
+
+int check_cfg(const Context &c, const bude_launch_cfg &cfg) {
+  const int p = cfg.ppwi;
+  if (p != 1 && p != 2 && p != 4 && p != 8 && p != 16)
+    return set_error(BUDE_ERR_ARG, "ppwi must be 1, 2, 4, 8 or 16 (got %d)", p);
+  if (cfg.wgsize < 32 || cfg.wgsize > kMaxThreads || cfg.wgsize % 32)
+    return set_error(BUDE_ERR_ARG, "wgsize must be a multiple of 32 in [32, %d] (got %d)", kMaxThreads, cfg.wgsize);
+  if (cfg.split < 1 || cfg.split > 8) return set_error(BUDE_ERR_ARG, "split must be in [1, 8] (got %d)", cfg.split);
+  if (cfg.tile < kAtomAlign || cfg.tile > 512 || cfg.tile % kAtomAlign)
+    return set_error(BUDE_ERR_ARG, "tile must be a multiple of %d in [%d, 512] (got %d)", kAtomAlign, kAtomAlign,
+                     cfg.tile);
+  if (exact_smem_bytes(p, cfg.wgsize, cfg.tile, cfg.split) > 200 * 1024)
+    return set_error(BUDE_ERR_ARG, "launch shape needs too much shared memory");
+  (void)c;
+  return BUDE_OK;
+}
+
+int default_cfg(const Context &c, int ppwi, int wgsize, bude_launch_cfg &cfg) {
+  cfg.ppwi = ppwi_to_p(std::max(ppwi, 1));
+  int w = wgsize < 32 ? 128 : round_up(wgsize, 32);
+  cfg.wgsize = std::min(w, kMaxThreads);
+  cfg.tile = 64;
+  // Enough blocks to give every SM several: split the protein when poses alone cannot.
+  const long long poses_per_block = (long long)cfg.ppwi * cfg.wgsize;
+  const long long blocks = std::max<long long>(1, (c.nposes + poses_per_block - 1) / poses_per_block);
+  const long long want = 4LL * std::max(c.num_sms, 1);
+  int split = 1;
+  while (split < 8 && blocks * split < want && (long long)c.natpro_pad / (split * 2) >= kAtomAlign) split *= 2;
+  cfg.split = split;
+  return BUDE_OK;
+}
+
+template <int P>
+static cudaError_t launch_exact_p(const ExactArgs &a, dim3 grid, int wgsize, size_t smem, int split,
+                                  cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(exact_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (split == 1) {
+    exact_kernel<P><<<grid, wgsize, smem, st>>>(a);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = grid;
+  lc.blockDim = dim3(wgsize, 1, 1);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 1;
+  attr[0].val.clusterDim.y = split;
+  attr[0].val.clusterDim.z = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, exact_kernel<P>, a);
+}
+
+// Enqueue one evaluation (pose transforms + exact kernel) on the context's stream; `mid`, when
+// given, is recorded between the two kernels.
+int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid) {
+  if (!c.have_deck) return set_error(BUDE_ERR_STATE, "no deck uploaded");
+  int rc = check_cfg(c, cfg);
+  if (rc) return rc;
+  if (c.nposes == 0) {
+    if (mid) cudaEventRecord(mid, c.stream);
+    return BUDE_OK;
+  }
+  {
+    const int tb = 256;
+    const long long nb = (c.nposes + tb - 1) / tb;
+    pose_xform_kernel<<<(unsigned)nb, tb, 0, c.stream>>>(c.poses.as<float>(), c.pose_stride, c.nposes,
+                                                         c.xform.as<float4>());
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "pose_xform_kernel launch");
+    c.launches++;
+  }
+  if (mid) cudaEventRecord(mid, c.stream);
+  ExactArgs a;
+  a.ligand = c.ligand.as<float4>();
+  a.slab = c.slab.as<float4>();
+  a.xform = c.xform.as<float>();
+  a.energies = c.energies.as<float>();
+  a.err = c.err.as<unsigned int>();
+  a.nposes = c.nposes;
+  a.natlig = c.natlig;
+  a.natpro_pad = c.natpro_pad;
+  a.tile = cfg.tile;
+  a.split = cfg.split;
+  a.slice = round_up((c.natpro_pad + cfg.split - 1) / cfg.split, kAtomAlign);
+  const long long ppb = (long long)cfg.ppwi * cfg.wgsize;
+  const long long nbx = (c.nposes + ppb - 1) / ppb;
+  if (nbx > 0x7fffffffLL) return set_error(BUDE_ERR_ARG, "too many poses for one launch");
+  dim3 grid((unsigned)nbx, (unsigned)cfg.split, 1);
+  const size_t smem = exact_smem_bytes(cfg.ppwi, cfg.wgsize, cfg.tile, cfg.split);
+  cudaError_t e;
+  switch (cfg.ppwi) {
+  case 1: e = launch_exact_p<1>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
+  case 2: e = launch_exact_p<2>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
+  case 4: e = launch_exact_p<4>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
+  case 8: e = launch_exact_p<8>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
+  default: e = launch_exact_p<16>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
+  }
+  if (e != cudaSuccess) return cuda_error(e, "exact_kernel launch");
+  c.launches++;
+  return BUDE_OK;
+}
+
+// Read (and clear) the device error word after the stream has drained.
+int check_device_error(Context &c) {
+  unsigned int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, c.err.ptr, sizeof h, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) return cuda_error(e, "device error word");
+  if (h) {
+    cudaMemsetAsync(c.err.ptr, 0, sizeof(unsigned int), c.stream);
+    cudaStreamSynchronize(c.stream);
+    return set_error(BUDE_ERR_TIMEOUT, "a bounded device wait ran out (error word 0x%x); energies are invalid", h);
+  }
+  return BUDE_OK;
+}
+
+static int upload_ligand(Context &c, const bude_atom *ligand, int natlig) {
+  for (int i = 0; i < natlig; ++i)
+    if (ligand[i].type < 0 || ligand[i].type >= c.ntypes)
+      return set_error(BUDE_ERR_TYPE, "ligand atom %d has type %d outside the forcefield (%d types)", i,
+                       ligand[i].type, c.ntypes);
+  int rc = c.ligand.reserve((size_t)std::max(natlig, 1) * 16, "ligand");
+  if (rc) return rc;
+  if (natlig > 0) {
+    // bude_atom is {x, y, z, int32 type}: the same 16 bytes as the kernel's float4 view.
+    cudaError_t e = cudaMemcpyAsync(c.ligand.ptr, ligand, (size_t)natlig * 16, cudaMemcpyHostToDevice, c.stream);
+    if (e != cudaSuccess) return cuda_error(e, "ligand upload");
+  }
+  c.natlig = natlig;
+  return BUDE_OK;
+}
+
+static int upload_poses(Context &c, const float *poses, long long stride, long long nposes) {
+  if (nposes < 0 || (nposes > 0 && (!poses || stride < nposes)))
+    return set_error(BUDE_ERR_ARG, "bad pose block (nposes %lld, stride %lld)", nposes, stride);
+  const long long n = std::max(nposes, 1LL);
+  int rc = c.poses.reserve((size_t)6 * n * sizeof(float), "poses");
+  if (!rc) rc = c.xform.reserve((size_t)12 * n * sizeof(float), "transforms");
+  if (!rc) rc = c.energies.reserve((size_t)n * sizeof(float), "energies");
+  if (rc) return rc;
+  if (nposes > 0) {
+    cudaError_t e = cudaMemcpy2DAsync(c.poses.ptr, (size_t)nposes * sizeof(float), poses, (size_t)stride * sizeof(float),
+                                      (size_t)nposes * sizeof(float), 6, cudaMemcpyHostToDevice, c.stream);
+    if (e != cudaSuccess) return cuda_error(e, "pose upload");
+  }
+  c.nposes = nposes;
+  c.pose_stride = nposes;
+  return BUDE_OK;
+}
+
+int upload_deck(Context &c, const bude_atom *protein, int natpro, const bude_atom *ligand, int natlig,
+                const bude_ffparams *ff, int ntypes, const float *poses, long long stride, long long nposes) {
+  c.have_deck = false; // a failed upload leaves no deck behind
+  if (natpro < 0 || natlig < 0 || ntypes <= 0 || !ff || (natpro > 0 && !protein) || (natlig > 0 && !ligand))
+    return set_error(BUDE_ERR_ARG, "bad deck sizes or pointers (natpro %d, natlig %d, ntypes %d)", natpro, natlig,
+                     ntypes);
+  for (int i = 0; i < natpro; ++i)
+    if (protein[i].type < 0 || protein[i].type >= ntypes)
+      return set_error(BUDE_ERR_TYPE, "protein atom %d has type %d outside the forcefield (%d types)", i,
+                       protein[i].type, ntypes);
+  c.ntypes = ntypes;
+  c.natpro = natpro;
+  c.natpro_pad = std::max(round_up(natpro, kAtomAlign), kAtomAlign);
+  std::vector<float> slab;
+  build_slab(protein, natpro, ff, ntypes, c.natpro_pad, slab);
+  int rc = c.slab.reserve(slab.size() * sizeof(float), "slab");
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(c.slab.ptr, slab.data(), slab.size() * sizeof(float), cudaMemcpyHostToDevice, c.stream);
+  if (e != cudaSuccess) return cuda_error(e, "slab upload");
+  // The host copy must stay alive until the async copy has read it.
+  e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) return cuda_error(e, "slab upload");
+  rc = upload_ligand(c, ligand, natlig);
+  if (!rc) rc = upload_poses(c, poses, stride, nposes);
+  if (rc) return rc;
+  e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) return cuda_error(e, "deck upload");
+  c.have_deck = true;
+  return BUDE_OK;
+}
+
+int set_poses(Context &c, const bude_atom *ligand, int natlig, const float *poses, long long stride,
+              long long nposes) {
+  if (!c.have_deck) return set_error(BUDE_ERR_STATE, "no deck uploaded");
+  int rc = BUDE_OK;
+  if (ligand) rc = upload_ligand(c, ligand, natlig);
+  if (!rc) rc = upload_poses(c, poses, stride, nposes);
+  return rc;
+}
+
+int make_context(int device, Context **out) {
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDeviceCount");
+  if (device < 0 || device >= count) return set_error(BUDE_ERR_ARG, "device %d out of range (%d devices)", device, count);
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  auto *c = new bude_gpu_ctx();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e != cudaSuccess) {
+    destroy_context(c);
+    return cuda_error(e, "stream/event creation");
+  }
+  int rc = c->err.reserve(sizeof(unsigned int) * 4, "error word");
+  if (!rc) {
+    e = cudaMemsetAsync(c->err.ptr, 0, sizeof(unsigned int) * 4, c->stream);
+    if (e != cudaSuccess) rc = cuda_error(e, "error word");
+  }
+  if (rc) {
+    destroy_context(c);
+    return rc;
+  }
+  *out = c;
+  return BUDE_OK;
+}
+
+void destroy_context(Context *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->ligand.release();
+  c->slab.release();
+  c->poses.release();
+  c->xform.release();
+  c->energies.release();
+  c->err.release();
+  c->flush.release();
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete static_cast<bude_gpu_ctx *>(c);
+}
+
+int flush_l2(Context &c) {
+  const size_t bytes = 512ull << 20; // well above the 126 MB L2
+  int rc = c.flush.reserve(bytes, "L2 flush buffer");
+  if (rc) return rc;
+  c.flush_gen = (c.flush_gen + 1) & 0xff;
+  cudaError_t e = cudaMemsetAsync(c.flush.ptr, c.flush_gen, bytes, c.stream);
+  if (e != cudaSuccess) return cuda_error(e, "L2 flush");
+  return BUDE_OK;
+}
+
+} // namespace bude
+
+// ---------------------------------------------------------------------------------------------
+// C-ABI
+
+extern "C" {
+
+const char *bude_gpu_last_error(void) { return bude::last_error(); }
+
+const char *bude_gpu_version(void) { return "minibude-gb300 0.1 (sm_103a)"; }
+
+int bude_gpu_device_count(int *count) {
+  if (!count) return set_error(BUDE_ERR_ARG, "count is NULL");
+  cudaError_t e = cudaGetDeviceCount(count);
+  if (e != cudaSuccess) {
+    *count = 0;
+    return cuda_error(e, "cudaGetDeviceCount");
+  }
+  return BUDE_OK;
+}
+
+int bude_gpu_device_name(int device, char *buf, size_t buflen) {
+  if (!buf || buflen == 0) return set_error(BUDE_ERR_ARG, "empty name buffer");
+  cudaDeviceProp p{};
+  cudaError_t e = cudaGetDeviceProperties(&p, device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDeviceProperties");
+  snprintf(buf, buflen, "%s (%zuMB;sm_%d%d)", p.name, (size_t)(p.totalGlobalMem / 1024 / 1024), p.major, p.minor);
+  return BUDE_OK;
+}
+
+int bude_gpu_sm_count(int device, int *sms) {
+  if (!sms) return set_error(BUDE_ERR_ARG, "sms is NULL");
+  cudaError_t e = cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, device);
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "cudaDeviceGetAttribute");
+}
+
+int bude_gpu_compatible(int device, int *kernel_cc, int *device_cc, int *ok) {
+  int kcc = 0;
+  int rc = bude::probe_kernel_arch(device, &kcc);
+  if (rc) return rc;
+  cudaDeviceProp p{};
+  cudaError_t e = cudaGetDeviceProperties(&p, device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDeviceProperties");
+  const int dcc = p.major * 10 + p.minor;
+  if (kernel_cc) *kernel_cc = kcc;
+  if (device_cc) *device_cc = dcc;
+  if (ok) *ok = kcc == dcc;
+  return BUDE_OK;
+}
+
+int bude_gpu_create(int device, bude_gpu_ctx **out) {
+  if (!out) return set_error(BUDE_ERR_ARG, "out is NULL");
+  bude::Context *c = nullptr;
+  int rc = bude::make_context(device, &c);
+  *out = static_cast<bude_gpu_ctx *>(c);
+  return rc;
+}
+
+int bude_gpu_destroy(bude_gpu_ctx *ctx) {
+  bude::destroy_context(ctx);
+  return BUDE_OK;
+}
+
+int bude_gpu_upload(bude_gpu_ctx *ctx, const bude_atom *protein, int32_t natpro, const bude_atom *ligand,
+                    int32_t natlig, const bude_ffparams *forcefield, int32_t ntypes, const float *poses,
+                    int64_t pose_stride, int64_t nposes) {
+  if (!ctx) return set_error(BUDE_ERR_ARG, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  return bude::upload_deck(*ctx, protein, natpro, ligand, natlig, forcefield, ntypes, poses, pose_stride, nposes);
+}
+
+int bude_gpu_set_poses(bude_gpu_ctx *ctx, const bude_atom *ligand, int32_t natlig, const float *poses,
+                       int64_t pose_stride, int64_t nposes) {
+  if (!ctx) return set_error(BUDE_ERR_ARG, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  int rc = bude::set_poses(*ctx, ligand, natlig, poses, pose_stride, nposes);
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "pose upload");
+}
+
+int bude_gpu_default_cfg(const bude_gpu_ctx *ctx, int32_t ppwi, int32_t wgsize, bude_launch_cfg *cfg) {
+  if (!ctx || !cfg) return set_error(BUDE_ERR_ARG, "NULL argument");
+  return bude::default_cfg(*ctx, ppwi, wgsize, *cfg);
+}
+
+int bude_gpu_run(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, float *kernel_ms) {
+  if (!ctx || !cfg) return set_error(BUDE_ERR_ARG, "NULL argument");
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaEventRecord(ctx->ev0, ctx->stream);
+  if (e != cudaSuccess) return cuda_error(e, "event record");
+  int rc = bude::enqueue_eval(*ctx, *cfg);
+  if (rc) return rc;
+  e = cudaEventRecord(ctx->ev1, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_error(e, "evaluation");
+  if (kernel_ms) {
+    e = cudaEventElapsedTime(kernel_ms, ctx->ev0, ctx->ev1);
+    if (e != cudaSuccess) return cuda_error(e, "event timing");
+  }
+  return bude::check_device_error(*ctx);
+}
+
+int bude_gpu_run_many(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, int32_t iterations, int32_t flush_l2,
+                      float *ms_per_iter, float *exact_ms_per_iter) {
+  if (!ctx || !cfg || iterations < 0) return set_error(BUDE_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  // Three events per iteration: start, after the pose transforms, after the exact kernel.
+  std::vector<cudaEvent_t> ev((size_t)iterations * 3, nullptr);
+  int rc = BUDE_OK;
+  cudaError_t e = cudaSuccess;
+  for (auto &x : ev)
+    if ((e = cudaEventCreate(&x)) != cudaSuccess) break;
+  if (e != cudaSuccess) rc = cuda_error(e, "event creation");
+  for (int i = 0; i < iterations && !rc; ++i) {
+    if (flush_l2) rc = bude::flush_l2(*ctx);
+    if (rc) break;
+    cudaEventRecord(ev[3 * i], ctx->stream);
+    rc = bude::enqueue_eval(*ctx, *cfg, ev[3 * i + 1]);
+    cudaEventRecord(ev[3 * i + 2], ctx->stream);
+  }
+  e = cudaStreamSynchronize(ctx->stream);
+  if (!rc && e != cudaSuccess) rc = cuda_error(e, "evaluation");
+  for (int i = 0; i < iterations && !rc; ++i) {
+    if (ms_per_iter) e = cudaEventElapsedTime(&ms_per_iter[i], ev[3 * i], ev[3 * i + 2]);
+    if (e == cudaSuccess && exact_ms_per_iter) e = cudaEventElapsedTime(&exact_ms_per_iter[i], ev[3 * i + 1], ev[3 * i + 2]);
+    if (e != cudaSuccess) rc = cuda_error(e, "event timing");
+  }
+  for (auto &x : ev)
+    if (x) cudaEventDestroy(x);
+  if (rc) return rc;
+  return bude::check_device_error(*ctx);
+}
+
+int bude_gpu_download(bude_gpu_ctx *ctx, float *energies, int64_t nposes) {
+  if (!ctx || (!energies && nposes > 0)) return set_error(BUDE_ERR_ARG, "NULL argument");
+  if (nposes != ctx->nposes)
+    return set_error(BUDE_ERR_ARG, "download of %lld energies but %lld poses are uploaded", (long long)nposes,
+                     ctx->nposes);
+  if (nposes == 0) return BUDE_OK;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaMemcpyAsync(energies, ctx->energies.ptr, (size_t)nposes * sizeof(float), cudaMemcpyDeviceToHost,
+                                  ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "energy download");
+}
+
+int bude_gpu_score_host(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, const bude_atom *ligand, int32_t natlig,
+                        const float *poses, int64_t pose_stride, int64_t nposes, float *energies) {
+  if (!ctx || !cfg || (!energies && nposes > 0)) return set_error(BUDE_ERR_ARG, "NULL argument");
+  cudaSetDevice(ctx->device);
+  int rc = bude::set_poses(*ctx, ligand, natlig, poses, pose_stride, nposes);
+  if (!rc) rc = bude::enqueue_eval(*ctx, *cfg);
+  if (rc) return rc;
+  if (nposes > 0) {
+    cudaError_t e = cudaMemcpyAsync(energies, ctx->energies.ptr, (size_t)nposes * sizeof(float),
+                                    cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return cuda_error(e, "energy download");
+  }
+  return bude::check_device_error(*ctx); // synchronises the stream
+}
+
+int bude_gpu_fasten(int device, int32_t ppwi, int32_t wgsize, const bude_atom *protein, int32_t natpro,
+                    const bude_atom *ligand, int32_t natlig, const bude_ffparams *forcefield, int32_t ntypes,
+                    const float *poses, int64_t pose_stride, int64_t nposes, int32_t iterations, float *energies,
+                    float *kernel_ms, float *context_ms) {
+  if (iterations < 1) return set_error(BUDE_ERR_ARG, "iterations must be >= 1");
+  bude_gpu_ctx *ctx = nullptr;
+  int rc = bude_gpu_create(device, &ctx);
+  if (rc) return rc;
+  auto t0 = std::chrono::steady_clock::now();
+  rc = bude_gpu_upload(ctx, protein, natpro, ligand, natlig, forcefield, ntypes, poses, pose_stride, nposes);
+  auto t1 = std::chrono::steady_clock::now();
+  if (context_ms) *context_ms = std::chrono::duration<float, std::milli>(t1 - t0).count();
+  bude_launch_cfg cfg;
+  if (!rc) rc = bude_gpu_default_cfg(ctx, ppwi, wgsize, &cfg);
+  for (int i = 0; i < iterations && !rc; ++i) rc = bude_gpu_run(ctx, &cfg, kernel_ms ? &kernel_ms[i] : nullptr);
+  if (!rc) rc = bude_gpu_download(ctx, energies, nposes);
+  std::string keep = rc ? bude::last_error() : "";
+  bude_gpu_destroy(ctx);
+  if (rc) bude::set_error(rc, "%s", keep.c_str());
+  return rc;
+}
+
+int bude_gpu_launch_count(const bude_gpu_ctx *ctx, int64_t *count) {
+  if (!ctx || !count) return set_error(BUDE_ERR_ARG, "NULL argument");
+  *count = ctx->launches;
+  return BUDE_OK;
+}
+
+int bude_host_alloc(size_t bytes, void **ptr) {
+  if (!ptr) return set_error(BUDE_ERR_ARG, "ptr is NULL");
+  cudaError_t e = cudaMallocHost(ptr, std::max<size_t>(bytes, 1));
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "cudaMallocHost");
+}
+
+int bude_host_free(void *ptr) {
+  cudaError_t e = cudaFreeHost(ptr);
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "cudaFreeHost");
+}
+
+} // extern "C"

@@ -1,0 +1,227 @@
+// exact_kernel.cuh -- the exact miniBUDE energy kernel for sm_103a.
+//
+// Computes, for every pose, the energy of reference `fasten_main` (src/cuda/fasten.hpp:20-161,
+// src/serial/fasten.hpp:18-132): the 3x4 pose transform, every ligand atom x every protein atom
+// steric + electrostatic + desolvation term, and 0.5 * the FP32 sum.
+//
+// Restatement of the pair energy.  For a ligand atom of type L and a protein atom of type P at
+// distance r (radij = radius_L + radius_P), the reference's three terms are piecewise linear in r
+// and each one is zero past its cut-off:
+//   steric   76 * (1 - r/radij)                      for r < radij
+//   charge   45*c * clamp(1 - (r - radij)/elcdst, 0, 1)  (c = elsc_L*elsc_P, sign forced negative
+//                                                    when either type is 'E'; elcdst 4 or 2)
+//   desolv   d * clamp(1 - (r - radij)/distdslv, 0, 1)   (d = signed hphb sum; zero unless the
+//                                                    protein hphb is non-zero and distdslv > 0)
+// The steric factor lies in [0, 1] as well (r >= 0), so all three are one `fma.rn.sat` each with
+// per-type-pair constants.  Those constants are folded into a per-ligand-type "slab" of protein
+// records built once per deck on the host (48 bytes per protein atom and ligand type):
+//   {px, py, pz, -1/radij,  -1/elcdst, 1 + radij/elcdst, -1/distdslv, 1 + radij/distdslv,
+//    45*c', d', 0, 0}
+// so one interaction is 3 FADD + FMUL + 2 FFMA (distance^2), one MUFU square root, 3 FFMA.SAT and
+// 3 FFMA (accumulate) -- 12 FP32 instructions against the reference's ~30 operations.
+//
+// Work decomposition.
+//   * each thread holds `P` poses (poses base + i*blockDim.x, i < P, strided like the reference,
+//     src/cuda/fasten.hpp:28,48,158): their transformed ligand atom and energy live in registers;
+//   * every warp walks the same (ligand atom, protein atom) sequence, so each protein record is a
+//     warp-uniform shared-memory broadcast (3 x LDS.128);
+//   * protein records stream through a `kStages`-deep ring of shared-memory stages filled by 1-D
+//     TMA bulk copies (cp.async.bulk) that complete on mbarriers, prefetched kStages-1 ahead;
+//   * blockIdx.y selects a protein slice; when the launch has split > 1 slices, the blocks of one
+//     pose block form a thread-block cluster along y and rank 0 sums the slices' partial energies
+//     from distributed shared memory in slice order (deterministic, no global scratch).
+#pragma once
+#include <cooperative_groups.h>
+#include <cstdint>
+
+#include "ptx.cuh"
+
+namespace bude {
+
+constexpr int kStages = 4;      // shared-memory ring depth
+constexpr int kRecF4 = 3;       // float4 per protein record (48 bytes)
+constexpr int kAtomAlign = 8;   // protein atoms are padded to a multiple of this (the unroll)
+constexpr float kSteric = 76.f; // 2 * HARDNESS (src/bude.h:32, serial/fasten.hpp:107)
+
+struct ExactArgs {
+  const float4 *ligand;   // natlig x {x, y, z, __int_as_float(type)}
+  const float4 *slab;     // ntypes x natpro_pad x kRecF4
+  const float *xform;     // nposes x 12 pose transforms (row-major 3x4, 48 bytes per pose)
+  float *energies;        // nposes
+  unsigned int *err;      // bit 0: a bounded wait ran out
+  long long nposes;
+  int natlig;
+  int natpro_pad;         // multiple of kAtomAlign
+  int tile;               // atoms per stage, multiple of kAtomAlign
+  int split;              // protein slices (cluster size along y)
+  int slice;              // atoms per slice, multiple of kAtomAlign
+};
+
+// Pose transforms: src/cuda/fasten.hpp:45-71 / serial/fasten.hpp:28-53, one thread per pose.
+// Output: three float4 rows per pose, {r00, r01, r02, tx}, {r10, r11, r12, ty}, {r20, r21, r22, tz}.
+__global__ void __launch_bounds__(256) pose_xform_kernel(const float *__restrict__ poses, long long pstride,
+                                                         long long nposes, float4 *__restrict__ xform) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nposes) return;
+  float sx, cx, sy, cy, sz, cz;
+  sincosf(poses[i], &sx, &cx);
+  sincosf(poses[pstride + i], &sy, &cy);
+  sincosf(poses[2 * pstride + i], &sz, &cz);
+  xform[3 * i + 0] = make_float4(cy * cz, sx * sy * cz - cx * sz, cx * sy * cz + sx * sz, poses[3 * pstride + i]);
+  xform[3 * i + 1] = make_float4(cy * sz, sx * sy * sz + cx * cz, cx * sy * sz - sx * cz, poses[4 * pstride + i]);
+  xform[3 * i + 2] = make_float4(-sy, sx * cy, cx * cy, poses[5 * pstride + i]);
+}
+
+// Dynamic shared memory of exact_kernel<P> for a launch shape.
+__host__ __device__ inline size_t exact_smem_bytes(int P, int wgsize, int tile, int split) {
+  size_t b = (size_t)kStages * tile * kRecF4 * sizeof(float4) + kStages * sizeof(uint64_t);
+  if (split > 1) b += (size_t)P * wgsize * sizeof(float);
+  return b;
+}
+
+constexpr int kMaxThreads = 512; // launch bound: keeps the register budget at 128 per thread
+
+template <int P>
+__global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  float4 *stages = reinterpret_cast<float4 *>(smem);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)kStages * a.tile * kRecF4 * sizeof(float4));
+  float *red = reinterpret_cast<float *>(full + kStages);
+
+  const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
+  const long long base = (long long)blockIdx.x * nthr * P + tid;
+
+  // Protein slice [a0, a1) of this block.
+  const int a0 = blockIdx.y * a.slice;
+  const int a1 = min(a.natpro_pad, a0 + a.slice);
+  const int natoms = max(0, a1 - a0);
+  const int ntile = (natoms + a.tile - 1) / a.tile;
+  const int Q = a.natlig * ntile; // (ligand atom, tile) steps
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  // Step q = il*ntile + k stages tile k of ligand atom il's slab row into stage q % kStages.
+  auto issue = [&](int q) {
+    const int il = q / ntile;
+    const int k = q - il * ntile;
+    const int lt = __float_as_int(__ldg(&a.ligand[il]).w);
+    const int first = a0 + k * a.tile;
+    const int cnt = min(a.tile, a1 - first);
+    const int s = q % kStages;
+    const uint32_t bytes = (uint32_t)cnt * kRecF4 * sizeof(float4);
+    mbar_arrive_expect_tx(&full[s], bytes);
+    bulk_g2s(stages + (size_t)s * a.tile * kRecF4, a.slab + ((size_t)lt * a.natpro_pad + first) * kRecF4, bytes,
+             &full[s]);
+  };
+  if (tid == 0)
+    for (int q = 0; q < min(kStages - 1, Q); ++q) issue(q);
+
+  float e[P], lx[P], ly[P], lz[P];
+#pragma unroll
+  for (int i = 0; i < P; ++i) e[i] = 0.f;
+
+  bool failed = false;
+  int q = 0;
+  for (; q < Q; ++q) {
+    const int il = q / ntile;
+    const int k = q - il * ntile;
+    if (k == 0) {
+      // Transform ligand atom il for each pose (serial/fasten.hpp:66-73).
+      const float4 la = __ldg(&a.ligand[il]);
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        long long pi = base + (long long)i * nthr;
+        pi = pi < a.nposes ? pi : a.nposes - 1;
+        // Re-read per ligand atom (volatile: the compiler must not keep 12*P transform values live
+        // across the protein loop); the block's transforms stay in L1.
+        const float4 *t = reinterpret_cast<const float4 *>(a.xform) + pi * 3;
+        const float4 r0 = ldg_stream(t + 0), r1 = ldg_stream(t + 1), r2 = ldg_stream(t + 2);
+        lx[i] = r0.w + la.x * r0.x + la.y * r0.y + la.z * r0.z;
+        ly[i] = r1.w + la.x * r1.x + la.y * r1.y + la.z * r1.z;
+        lz[i] = r2.w + la.x * r2.x + la.y * r2.y + la.z * r2.z;
+      }
+    }
+    // Everyone is done with step q-1, so its stage may be refilled; agree on failure first.
+    if (__syncthreads_or(failed)) break;
+    if (tid == 0 && q + kStages - 1 < Q) issue(q + kStages - 1);
+    const int s = q % kStages;
+    if (!mbar_wait_bounded(&full[s], (uint32_t)(q / kStages) & 1u)) {
+      failed = true;
+      continue;
+    }
+    const float4 *sp = stages + (size_t)s * a.tile * kRecF4;
+    const int cnt = min(a.tile, a1 - (a0 + k * a.tile));
+    // Unroll over U atoms so one unrolled body holds about 16 interactions per thread: enough
+    // independent work to hide latency without the compiler hoisting every record into registers.
+    constexpr int U = P >= 16 ? 1 : (16 / P > kAtomAlign ? kAtomAlign : 16 / P);
+#pragma unroll 1
+    for (int j = 0; j < cnt; j += U) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float4 A = sp[(j + u) * kRecF4 + 0]; // px py pz -1/radij
+        const float4 B = sp[(j + u) * kRecF4 + 1]; // -1/elcdst b_chrg -1/distdslv b_dslv
+        const float4 C = sp[(j + u) * kRecF4 + 2]; // k_chrg k_dslv
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+          const float dx = lx[i] - A.x;
+          const float dy = ly[i] - A.y;
+          const float dz = lz[i] - A.z;
+          float d2 = dx * dx;
+          d2 = fmaf(dy, dy, d2);
+          d2 = fmaf(dz, dz, d2);
+          const float r = sqrt_approx(d2);
+          const float fs = fma_sat(r, A.w, 1.f);
+          const float fc = fma_sat(r, B.x, B.y);
+          const float fd = fma_sat(r, B.z, B.w);
+          e[i] = fmaf(fs, kSteric, e[i]);
+          e[i] = fmaf(fc, C.x, e[i]);
+          e[i] = fmaf(fd, C.y, e[i]);
+        }
+      }
+    }
+  }
+
+  // A wait that ran out on any thread (including in the last step) fails the whole block.
+  const bool ok = !__syncthreads_or(failed || q < Q);
+  if (!ok && tid == 0) {
+    // Record it, then wait (bounded) for this block's copies that may still be in flight -- steps
+    // q-1 .. q+kStages-2 -- so no bulk copy lands in shared memory after the block has exited.
+    atomicOr(a.err, 1u);
+    for (int d = max(0, q - 1); d < min(Q, q + kStages - 1); ++d)
+      (void)mbar_wait_bounded(&full[d % kStages], (uint32_t)(d / kStages) & 1u);
+  }
+
+  if (a.split == 1) {
+    if (!ok) return;
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      const long long pi = base + (long long)i * nthr;
+      if (pi < a.nposes) a.energies[pi] = 0.5f * e[i];
+    }
+    return;
+  }
+
+  // Cluster reduction over protein slices (every block of the cluster reaches both barriers).
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+#pragma unroll
+  for (int i = 0; i < P; ++i) red[i * nthr + tid] = e[i];
+  cluster.sync();
+  if (blockIdx.y == 0 && ok) {
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      float acc = red[i * nthr + tid];
+      for (int r = 1; r < a.split; ++r) acc += cluster.map_shared_rank(red, r)[i * nthr + tid];
+      const long long pi = base + (long long)i * nthr;
+      if (pi < a.nposes) a.energies[pi] = 0.5f * acc;
+    }
+  }
+  cluster.sync();
+}
+
+} // namespace bude

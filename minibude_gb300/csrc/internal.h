@@ -1,0 +1,65 @@
+// internal.h -- shared host-side declarations of libbude_gb300.so (not part of the C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <vector>
+
+#include "../../include/minibude_gb300.h"
+
+namespace bude {
+
+// Reference constants used by the host-side pair set-up (src/bude.h:22-35).
+constexpr int kHbtypeF = 70;
+constexpr int kHbtypeE = 69;
+constexpr float kCnstnt = 45.0f;
+constexpr float kNpNpDist = 5.5f;
+constexpr float kNpPDist = 1.0f;
+
+// A growable device allocation.
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t cap = 0;
+  int reserve(size_t nbytes, const char *what);
+  void release();
+  template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// State behind a bude_gpu_ctx handle.
+struct Context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // deck
+  bool have_deck = false;
+  int natpro = 0, natpro_pad = 0, natlig = 0, ntypes = 0;
+  long long nposes = 0, pose_stride = 0;
+  DevBuf ligand, slab, poses, xform, energies, err, flush;
+  int flush_gen = 0;
+  long long launches = 0;
+};
+
+int set_error(int code, const char *fmt, ...);
+int cuda_error(cudaError_t e, const char *what);
+const char *last_error();
+
+void pair_record(const bude_ffparams &L, const bude_ffparams &P, float px, float py, float pz, float *rec);
+void null_record(float *rec);
+void build_slab(const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes, int natpro_pad,
+                std::vector<float> &slab);
+
+int make_context(int device, Context **out);
+void destroy_context(Context *c);
+int upload_deck(Context &c, const bude_atom *protein, int natpro, const bude_atom *ligand, int natlig,
+                const bude_ffparams *ff, int ntypes, const float *poses, long long stride, long long nposes);
+int set_poses(Context &c, const bude_atom *ligand, int natlig, const float *poses, long long stride,
+              long long nposes);
+int check_cfg(const Context &c, const bude_launch_cfg &cfg);
+int default_cfg(const Context &c, int ppwi, int wgsize, bude_launch_cfg &cfg);
+int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid = nullptr);
+int check_device_error(Context &c);
+int flush_l2(Context &c);
+int probe_kernel_arch(int device, int *cc);
+
+} // namespace bude

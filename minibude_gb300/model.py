@@ -1,0 +1,224 @@
+"""Python host mirror of the reference's model interface, over the C-ABI.
+
+`Gb300Bude` has the shape of `Bude<PPWI>` (src/bude.h:95-101): `name`, `enumerate_devices`,
+`compatible` and `fasten`, with the reference's semantics -- `fasten` owns every device
+allocation of the call, runs `iterations + warmup` evaluations and returns a `Sample` whose
+energies are in pose order and whose kernel times include the warm-ups (src/main.cpp:344-351).
+`GpuContext` is the lower-level handle used by the benchmark and the tests.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import time
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import capi
+from .capi import BudeLaunchCfg, check, fptr, ptr
+from .deck import ATOM_DTYPE, FF_DTYPE, Deck
+
+
+def _atoms(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=ATOM_DTYPE)
+
+
+def _ff(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=FF_DTYPE)
+
+
+def _poses(p) -> np.ndarray:
+    p = np.ascontiguousarray(p, dtype=np.float32)
+    if p.ndim != 2 or p.shape[0] != 6:
+        raise ValueError("poses must be a float32 [6, nposes] block")
+    return p
+
+
+def launch_cfg(ppwi: int, wgsize: int, split: int = 1, tile: int = 64) -> BudeLaunchCfg:
+    return BudeLaunchCfg(ppwi, wgsize, split, tile)
+
+
+class GpuContext:
+    """One bude_gpu_ctx: a device, a stream and an uploaded deck."""
+
+    def __init__(self, device: int = 0):
+        self._lib = capi.lib()
+        h = ctypes.c_void_p()
+        check(self._lib.bude_gpu_create(device, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+        self.nposes = 0
+        self._keep = []
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.bude_gpu_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, deck: Deck) -> None:
+        protein, ligand, ff = _atoms(deck.protein), _atoms(deck.ligand), _ff(deck.forcefield)
+        poses = _poses(deck.poses)
+        check(self._lib.bude_gpu_upload(self.handle, ptr(protein), protein.size, ptr(ligand), ligand.size, ptr(ff),
+                                        ff.size, ptr(poses), poses.shape[1], poses.shape[1]))
+        self.nposes = poses.shape[1]
+
+    def set_poses(self, poses: np.ndarray, ligand: Optional[np.ndarray] = None) -> None:
+        poses = _poses(poses)
+        lig = None if ligand is None else _atoms(ligand)
+        check(self._lib.bude_gpu_set_poses(self.handle, ptr(lig), 0 if lig is None else lig.size, ptr(poses),
+                                           poses.shape[1], poses.shape[1]))
+        self.nposes = poses.shape[1]
+
+    def default_cfg(self, ppwi: int, wgsize: int) -> BudeLaunchCfg:
+        cfg = BudeLaunchCfg()
+        check(self._lib.bude_gpu_default_cfg(self.handle, ppwi, wgsize, ctypes.byref(cfg)))
+        return cfg
+
+    def run(self, cfg: BudeLaunchCfg) -> float:
+        ms = ctypes.c_float()
+        check(self._lib.bude_gpu_run(self.handle, ctypes.byref(cfg), ctypes.byref(ms)))
+        return ms.value
+
+    def run_many(self, cfg: BudeLaunchCfg, iterations: int, flush_l2: bool = True):
+        """(per-evaluation ms, exact-kernel-only ms) for `iterations` timed evaluations."""
+        out = np.zeros(max(iterations, 1), np.float32)
+        exact = np.zeros(max(iterations, 1), np.float32)
+        check(self._lib.bude_gpu_run_many(self.handle, ctypes.byref(cfg), iterations, int(flush_l2), fptr(out),
+                                          fptr(exact)))
+        return out[:iterations], exact[:iterations]
+
+    def download(self) -> np.ndarray:
+        out = np.zeros(self.nposes, np.float32)
+        check(self._lib.bude_gpu_download(self.handle, fptr(out), self.nposes))
+        return out
+
+    def score_host(self, cfg: BudeLaunchCfg, poses: np.ndarray, energies: np.ndarray,
+                   ligand: Optional[np.ndarray] = None) -> np.ndarray:
+        """End to end from host buffers: poses (and ligand) in, energies out."""
+        poses = _poses(poses)
+        lig = None if ligand is None else _atoms(ligand)
+        check(self._lib.bude_gpu_score_host(self.handle, ctypes.byref(cfg), ptr(lig),
+                                            0 if lig is None else lig.size, ptr(poses), poses.shape[1],
+                                            poses.shape[1], fptr(energies)))
+        self.nposes = poses.shape[1]
+        return energies
+
+    def launch_count(self) -> int:
+        n = ctypes.c_int64()
+        check(self._lib.bude_gpu_launch_count(self.handle, ctypes.byref(n)))
+        return n.value
+
+    def energies(self, deck: Deck, cfg: Optional[BudeLaunchCfg] = None) -> np.ndarray:
+        """Upload, evaluate once and download: the energies of every pose of `deck`."""
+        self.upload(deck)
+        if cfg is None:
+            cfg = self.default_cfg(8, 128)
+        self.run(cfg)
+        return self.download()
+
+
+class PinnedBuffer:
+    """Page-locked host memory viewed as a numpy array."""
+
+    def __init__(self, shape, dtype=np.float32):
+        self._lib = capi.lib()
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        p = ctypes.c_void_p()
+        check(self._lib.bude_host_alloc(nbytes, ctypes.byref(p)))
+        self._p = p
+        buf = (ctypes.c_byte * max(nbytes, 1)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if self._p:
+            self.array = None
+            self._lib.bude_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+@dataclasses.dataclass
+class Sample:
+    """src/bude.h:84-91: per-call results of `fasten`."""
+    ppwi: int
+    wgsize: int
+    energies: np.ndarray
+    kernel_times: List[Tuple[float, float]]  # host clock (start, end) per iteration, seconds
+    kernel_ms: List[float]  # CUDA-event time per iteration
+    context_time: Optional[Tuple[float, float]] = None
+
+
+def device_count() -> int:
+    n = ctypes.c_int()
+    check(capi.lib().bude_gpu_device_count(ctypes.byref(n)))
+    return n.value
+
+
+def sm_count(device: int) -> int:
+    n = ctypes.c_int()
+    check(capi.lib().bude_gpu_sm_count(device, ctypes.byref(n)))
+    return n.value
+
+
+def device_name(device: int) -> str:
+    buf = ctypes.create_string_buffer(256)
+    check(capi.lib().bude_gpu_device_name(device, buf, len(buf)))
+    return buf.value.decode()
+
+
+class Gb300Bude:
+    """The GB300 model behind the reference's `Bude<PPWI>` interface."""
+
+    def __init__(self, ppwi: int = 1):
+        self.ppwi = int(ppwi)
+
+    def name(self) -> str:
+        return "gb300"
+
+    def enumerate_devices(self) -> List[Tuple[int, str]]:
+        """src/cuda/fasten.hpp:181-196."""
+        return [(i, device_name(i)) for i in range(device_count())]
+
+    def compatible(self, deck: Deck, wgsize: int, device: int) -> bool:
+        """src/cuda/fasten.hpp:218-248: kernel and device compute capabilities agree."""
+        k, d, ok = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(capi.lib().bude_gpu_compatible(device, ctypes.byref(k), ctypes.byref(d), ctypes.byref(ok)))
+        return bool(ok.value)
+
+    def fasten(self, deck: Deck, wgsize: int, device: int, iterations: int = 8, warmup: int = 2) -> Sample:
+        """src/cuda/fasten.hpp:250-305: allocate + copy (context), run iterations + warm-ups
+        with a synchronise after each, copy the energies back, free."""
+        t0 = time.perf_counter()
+        ctx = GpuContext(device)
+        try:
+            ctx.upload(deck)
+            t1 = time.perf_counter()
+            cfg = ctx.default_cfg(self.ppwi, wgsize)
+            times, ms = [], []
+            for _ in range(iterations + warmup):
+                s = time.perf_counter()
+                ms.append(ctx.run(cfg))
+                times.append((s, time.perf_counter()))
+            energies = ctx.download()
+        finally:
+            ctx.close()
+        return Sample(self.ppwi, wgsize, energies, times, ms, (t0, t1))
