@@ -50,7 +50,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["large", "small"], default="large")
-    ap.add_argument("--cfg", default="auto", help="auto, or ppwi,wgsize,split,tile")
+    ap.add_argument("--cfg", default="auto", help="auto, or ppwi,wgsize,split,tile[,unroll]")
+    ap.add_argument("--nposes", type=int, default=0, help="use the first N poses of the deck (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -192,13 +193,10 @@ def cpu_sample_run(deck, seconds: float, fast: bool = True):
 def parse_cfg(ctx, text: str, deck):
     from minibude_gb300.model import launch_cfg
     if text != "auto":
-        p, w, s, t = (int(x) for x in text.split(","))
-        return launch_cfg(p, w, s, t)
-    try:
-        from minibude_gb300 import tune
-        return tune.pick(ctx, deck)
-    except ImportError:
-        return ctx.default_cfg(8, 128)
+        vals = [int(x) for x in text.split(",")]
+        return launch_cfg(*vals)
+    cfg, _ = ctx.autotune()
+    return cfg
 
 
 def run_ours(args, dist: Dist):
@@ -206,7 +204,7 @@ def run_ours(args, dist: Dist):
     from minibude_gb300.model import GpuContext, PinnedBuffer
     build.build_library()
     spec = LARGE if args.workload == "large" else SMALL
-    deck = synthetic_deck(spec, seed=dist.rank)
+    deck = synthetic_deck(spec, seed=dist.rank, nposes=args.nposes or None)
     peaks = measured_peaks()
     ctx = GpuContext(dist.local_rank)
     ctx.upload(deck)

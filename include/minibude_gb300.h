@@ -46,10 +46,13 @@ typedef struct bude_ffparams {
  * item, a template parameter, src/main.cpp:48-53) and wgsize (threads per block,
  * src/cuda/fasten.hpp:272-275); this kernel adds the protein split and the shared-memory tile. */
 typedef struct bude_launch_cfg {
-  int32_t ppwi;   /* poses per thread, held in registers: 1, 2, 4, 8 or 16 */
-  int32_t wgsize; /* threads per block: a multiple of 32 in [32, 512] */
-  int32_t split;  /* protein slices per pose block, reduced across a thread-block cluster: 1..8 */
-  int32_t tile;   /* protein atoms per shared-memory stage (TMA bulk copy): multiple of 8, 8..512 */
+  int32_t ppwi;    /* poses per thread, held in registers: 1, 2, 4, 8 or 16 */
+  int32_t wgsize;  /* threads per block: a multiple of 32 in [32, 512] */
+  int32_t split;   /* protein slices per pose block: 1..8 with cluster = 1, 1..64 with cluster = 0 */
+  int32_t tile;    /* protein atoms per shared-memory stage (TMA bulk copy): multiple of 8, 8..512 */
+  int32_t unroll;  /* protein atoms per unrolled inner-loop body: 1, 2 or 4 */
+  int32_t cluster; /* split > 1: 1 = slices summed inside a thread-block cluster (distributed shared
+                      memory), 0 = through a context-owned [split][nposes] buffer and a second kernel */
 } bude_launch_cfg;
 
 typedef struct bude_gpu_ctx bude_gpu_ctx;
@@ -94,6 +97,13 @@ int bude_gpu_set_poses(bude_gpu_ctx *ctx, const bude_atom *ligand, int32_t natli
  * for the uploaded deck.  PPWI above 16 uses 16 poses per thread; wgsize 0 or below 32 is rounded
  * up to a multiple of 32.  Results do not depend on the shape beyond FP32 summation order. */
 int bude_gpu_default_cfg(const bude_gpu_ctx *ctx, int32_t ppwi, int32_t wgsize, bude_launch_cfg *cfg);
+
+/* Choose a launch shape for the uploaded deck by measurement; replaces the reference driver's
+ * brute-force PPWI x wgsize sweep (src/main.cpp:517-541).  Candidate shapes get their protein
+ * split from a wave model (resident blocks per SM from the occupancy API) and are timed with CUDA
+ * events on a ligand prefix, within about max_ms of GPU time.  The pick is cached per deck shape
+ * in the context.  best_ms (optional) receives the predicted time of one full evaluation. */
+int bude_gpu_autotune(bude_gpu_ctx *ctx, int32_t max_ms, bude_launch_cfg *best, float *best_ms);
 
 /* One evaluation of all uploaded poses (one iteration of the reference's hot loop,
  * src/cuda/fasten.hpp:277-286): pose transforms and the exact kernel on the context's stream,

@@ -31,10 +31,12 @@ STATUS_NAMES = {
 
 
 class BudeLaunchCfg(ctypes.Structure):
-    _fields_ = [("ppwi", c_int32), ("wgsize", c_int32), ("split", c_int32), ("tile", c_int32)]
+    _fields_ = [("ppwi", c_int32), ("wgsize", c_int32), ("split", c_int32), ("tile", c_int32), ("unroll", c_int32),
+                ("cluster", c_int32)]
 
     def as_dict(self):
-        return {"ppwi": self.ppwi, "wgsize": self.wgsize, "split": self.split, "tile": self.tile}
+        return {"ppwi": self.ppwi, "wgsize": self.wgsize, "split": self.split, "tile": self.tile,
+                "unroll": self.unroll, "cluster": self.cluster}
 
     def __repr__(self):
         return "BudeLaunchCfg(%s)" % ", ".join(f"{k}={v}" for k, v in self.as_dict().items())
@@ -61,6 +63,7 @@ SIGNATURES = [
     ("bude_gpu_upload", ctypes.c_int, [_P, _P, c_int32, _P, c_int32, _P, c_int32, _P, c_int64, c_int64]),
     ("bude_gpu_set_poses", ctypes.c_int, [_P, _P, c_int32, _P, c_int64, c_int64]),
     ("bude_gpu_default_cfg", ctypes.c_int, [_P, c_int32, c_int32, ctypes.POINTER(BudeLaunchCfg)]),
+    ("bude_gpu_autotune", ctypes.c_int, [_P, c_int32, ctypes.POINTER(BudeLaunchCfg), c_float_p]),
     ("bude_gpu_run", ctypes.c_int, [_P, ctypes.POINTER(BudeLaunchCfg), c_float_p]),
     ("bude_gpu_run_many", ctypes.c_int, [_P, ctypes.POINTER(BudeLaunchCfg), c_int32, c_int32, c_float_p,
                                          c_float_p]),

@@ -60,41 +60,39 @@ void pair_record(const bude_ffparams &L, const bude_ffparams &Pp, float px, floa
   const double r_distdslv = dslv_on ? 1.0 / (double)distdslv : 1.0;
   const float chrg_init = L.elsc * Pp.elsc;
   const float dslv_init = p_hphb + l_hphb;
-  rec[0] = px;
-  rec[1] = py;
-  rec[2] = pz;
-  rec[3] = (float)(-1.0 / (double)radij);
-  rec[4] = (float)(-elcdst1);
-  rec[5] = (float)(1.0 + (double)radij * elcdst1);
-  rec[6] = (float)(-r_distdslv);
-  rec[7] = dslv_on ? (float)(1.0 + (double)radij * r_distdslv) : 0.f;
-  rec[8] = kCnstnt * (type_e ? -std::fabs(chrg_init) : chrg_init);
-  rec[9] = dslv_on ? dslv_init : 0.f;
-  rec[10] = 0.f;
-  rec[11] = 0.f;
+  const float k_chrg = kCnstnt * (type_e ? -std::fabs(chrg_init) : chrg_init);
+  const float k_dslv = dslv_on ? dslv_init : 0.f;
+  rec[0] = rec[1] = px;
+  rec[2] = rec[3] = py;
+  rec[4] = rec[5] = pz;
+  rec[6] = rec[7] = k_chrg;
+  rec[8] = rec[9] = k_dslv;
+  rec[10] = (float)(-1.0 / (double)radij);
+  rec[11] = (float)(-elcdst1);
+  rec[12] = (float)(1.0 + (double)radij * elcdst1);
+  rec[13] = (float)(-r_distdslv);
+  rec[14] = dslv_on ? (float)(1.0 + (double)radij * r_distdslv) : 0.f;
+  rec[15] = 0.f;
 }
 
 // A padding atom: far away (every saturating factor is 0) with zero charge/desolvation weights.
 void null_record(float *rec) {
   const float far = 1.0e15f;
-  rec[0] = rec[1] = rec[2] = far;
-  rec[3] = -1.f;
-  rec[4] = -1.f;
-  rec[5] = 0.f;
-  rec[6] = -1.f;
-  rec[7] = 0.f;
-  rec[8] = rec[9] = rec[10] = rec[11] = 0.f;
+  for (int i = 0; i < 6; ++i) rec[i] = far;
+  for (int i = 6; i < 10; ++i) rec[i] = 0.f;
+  rec[10] = rec[11] = rec[13] = -1.f;
+  rec[12] = rec[14] = rec[15] = 0.f;
 }
 
 // slab[t][j] = record for ligand type t against protein atom j; rows padded to natpro_pad.
 void build_slab(const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes, int natpro_pad,
                 std::vector<float> &slab) {
-  slab.assign((size_t)ntypes * natpro_pad * 12, 0.f);
+  slab.assign((size_t)ntypes * natpro_pad * kRecFloats, 0.f);
   for (int t = 0; t < ntypes; ++t) {
-    float *row = slab.data() + (size_t)t * natpro_pad * 12;
+    float *row = slab.data() + (size_t)t * natpro_pad * kRecFloats;
     for (int j = 0; j < natpro; ++j)
-      pair_record(ff[t], ff[protein[j].type], protein[j].x, protein[j].y, protein[j].z, row + (size_t)j * 12);
-    for (int j = natpro; j < natpro_pad; ++j) null_record(row + (size_t)j * 12);
+      pair_record(ff[t], ff[protein[j].type], protein[j].x, protein[j].y, protein[j].z, row + (size_t)j * kRecFloats);
+    for (int j = natpro; j < natpro_pad; ++j) null_record(row + (size_t)j * kRecFloats);
   }
 }
 
@@ -121,7 +119,6 @@ void DevBuf::release() {
 
 using namespace bude;
 
-struct bude_gpu_ctx : public bude::Context {};
 
 // ---------------------------------------------------------------------------------------------
 // Launch helpers
@@ -130,52 +127,33 @@ namespace bude {
 
 static int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
-static int ppwi_to_p(int ppwi) {
-  if (ppwi >= 16) return 16;
-  if (ppwi >= 8) return 8;
-  if (ppwi >= 4) return 4;
-  if (ppwi >= 2) return 2;
-  return 1;
-}
-
 int check_cfg(const Context &c, const bude_launch_cfg &cfg) {
   const int p = cfg.ppwi;
   if (p != 1 && p != 2 && p != 4 && p != 8 && p != 16)
     return set_error(BUDE_ERR_ARG, "ppwi must be 1, 2, 4, 8 or 16 (got %d)", p);
   if (cfg.wgsize < 32 || cfg.wgsize > kMaxThreads || cfg.wgsize % 32)
     return set_error(BUDE_ERR_ARG, "wgsize must be a multiple of 32 in [32, %d] (got %d)", kMaxThreads, cfg.wgsize);
-  if (cfg.split < 1 || cfg.split > 8) return set_error(BUDE_ERR_ARG, "split must be in [1, 8] (got %d)", cfg.split);
+  if (cfg.cluster != 0 && cfg.cluster != 1) return set_error(BUDE_ERR_ARG, "cluster must be 0 or 1 (got %d)", cfg.cluster);
+  if (cfg.split < 1 || cfg.split > (cfg.cluster ? 8 : 64))
+    return set_error(BUDE_ERR_ARG, "split must be in [1, %d] (got %d)", cfg.cluster ? 8 : 64, cfg.split);
   if (cfg.tile < kAtomAlign || cfg.tile > 512 || cfg.tile % kAtomAlign)
     return set_error(BUDE_ERR_ARG, "tile must be a multiple of %d in [%d, 512] (got %d)", kAtomAlign, kAtomAlign,
                      cfg.tile);
-  if (exact_smem_bytes(p, cfg.wgsize, cfg.tile, cfg.split) > 200 * 1024)
+  if (cfg.unroll != 1 && cfg.unroll != 2 && cfg.unroll != 4)
+    return set_error(BUDE_ERR_ARG, "unroll must be 1, 2 or 4 (got %d)", cfg.unroll);
+  if (exact_smem_bytes(p, cfg.wgsize, cfg.tile, cfg.split, cfg.cluster) > 200 * 1024)
     return set_error(BUDE_ERR_ARG, "launch shape needs too much shared memory");
   (void)c;
   return BUDE_OK;
 }
 
-int default_cfg(const Context &c, int ppwi, int wgsize, bude_launch_cfg &cfg) {
-  cfg.ppwi = ppwi_to_p(std::max(ppwi, 1));
-  int w = wgsize < 32 ? 128 : round_up(wgsize, 32);
-  cfg.wgsize = std::min(w, kMaxThreads);
-  cfg.tile = 64;
-  // Enough blocks to give every SM several: split the protein when poses alone cannot.
-  const long long poses_per_block = (long long)cfg.ppwi * cfg.wgsize;
-  const long long blocks = std::max<long long>(1, (c.nposes + poses_per_block - 1) / poses_per_block);
-  const long long want = 4LL * std::max(c.num_sms, 1);
-  int split = 1;
-  while (split < 8 && blocks * split < want && (long long)c.natpro_pad / (split * 2) >= kAtomAlign) split *= 2;
-  cfg.split = split;
-  return BUDE_OK;
-}
-
-template <int P>
-static cudaError_t launch_exact_p(const ExactArgs &a, dim3 grid, int wgsize, size_t smem, int split,
-                                  cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(exact_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int P, int U>
+static cudaError_t launch_exact_pu(const ExactArgs &a, dim3 grid, int wgsize, size_t smem, int split,
+                                   cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(exact_kernel<P, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  if (split == 1) {
-    exact_kernel<P><<<grid, wgsize, smem, st>>>(a);
+  if (split == 1 || !a.cluster) {
+    exact_kernel<P, U><<<grid, wgsize, smem, st>>>(a);
     return cudaGetLastError();
   }
   cudaLaunchConfig_t lc = {};
@@ -190,7 +168,42 @@ static cudaError_t launch_exact_p(const ExactArgs &a, dim3 grid, int wgsize, siz
   attr[0].val.clusterDim.z = 1;
   lc.attrs = attr;
   lc.numAttrs = 1;
-  return cudaLaunchKernelEx(&lc, exact_kernel<P>, a);
+  return cudaLaunchKernelEx(&lc, exact_kernel<P, U>, a);
+}
+
+template <int P>
+static cudaError_t launch_exact_p(const ExactArgs &a, dim3 grid, const bude_launch_cfg &cfg, size_t smem,
+                                  cudaStream_t st) {
+  switch (cfg.unroll) {
+  case 1: return launch_exact_pu<P, 1>(a, grid, cfg.wgsize, smem, cfg.split, st);
+  case 2: return launch_exact_pu<P, 2>(a, grid, cfg.wgsize, smem, cfg.split, st);
+  default: return launch_exact_pu<P, 4>(a, grid, cfg.wgsize, smem, cfg.split, st);
+  }
+}
+
+template <int P, int U> static int blocks_per_sm_pu(int wgsize, size_t smem, int *out) {
+  cudaError_t e = cudaFuncSetAttribute(exact_kernel<P, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, exact_kernel<P, U>, wgsize, smem);
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "occupancy query");
+}
+
+template <int P> static int blocks_per_sm_p(const bude_launch_cfg &cfg, size_t smem, int *out) {
+  switch (cfg.unroll) {
+  case 1: return blocks_per_sm_pu<P, 1>(cfg.wgsize, smem, out);
+  case 2: return blocks_per_sm_pu<P, 2>(cfg.wgsize, smem, out);
+  default: return blocks_per_sm_pu<P, 4>(cfg.wgsize, smem, out);
+  }
+}
+
+int exact_blocks_per_sm(const bude_launch_cfg &cfg, int *out) {
+  const size_t smem = exact_smem_bytes(cfg.ppwi, cfg.wgsize, cfg.tile, cfg.split, cfg.cluster);
+  switch (cfg.ppwi) {
+  case 1: return blocks_per_sm_p<1>(cfg, smem, out);
+  case 2: return blocks_per_sm_p<2>(cfg, smem, out);
+  case 4: return blocks_per_sm_p<4>(cfg, smem, out);
+  case 8: return blocks_per_sm_p<8>(cfg, smem, out);
+  default: return blocks_per_sm_p<16>(cfg, smem, out);
+  }
 }
 
 // Enqueue one evaluation (pose transforms + exact kernel) on the context's stream; `mid`, when
@@ -218,28 +231,45 @@ int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid) {
   a.slab = c.slab.as<float4>();
   a.xform = c.xform.as<float>();
   a.energies = c.energies.as<float>();
+  a.partial = nullptr;
   a.err = c.err.as<unsigned int>();
   a.nposes = c.nposes;
   a.natlig = c.natlig;
   a.natpro_pad = c.natpro_pad;
   a.tile = cfg.tile;
   a.split = cfg.split;
+  a.cluster = cfg.cluster;
+  const bool global_reduce = cfg.split > 1 && !cfg.cluster;
+  if (global_reduce) {
+    // Slice sums go through a [split][nposes] buffer owned by the context.
+    int rc2 = c.partial.reserve((size_t)cfg.split * c.nposes * sizeof(float), "slice partial sums");
+    if (rc2) return rc2;
+    a.partial = c.partial.as<float>();
+  }
   a.slice = round_up((c.natpro_pad + cfg.split - 1) / cfg.split, kAtomAlign);
   const long long ppb = (long long)cfg.ppwi * cfg.wgsize;
   const long long nbx = (c.nposes + ppb - 1) / ppb;
   if (nbx > 0x7fffffffLL) return set_error(BUDE_ERR_ARG, "too many poses for one launch");
   dim3 grid((unsigned)nbx, (unsigned)cfg.split, 1);
-  const size_t smem = exact_smem_bytes(cfg.ppwi, cfg.wgsize, cfg.tile, cfg.split);
+  const size_t smem = exact_smem_bytes(cfg.ppwi, cfg.wgsize, cfg.tile, cfg.split, cfg.cluster);
   cudaError_t e;
   switch (cfg.ppwi) {
-  case 1: e = launch_exact_p<1>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
-  case 2: e = launch_exact_p<2>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
-  case 4: e = launch_exact_p<4>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
-  case 8: e = launch_exact_p<8>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
-  default: e = launch_exact_p<16>(a, grid, cfg.wgsize, smem, cfg.split, c.stream); break;
+  case 1: e = launch_exact_p<1>(a, grid, cfg, smem, c.stream); break;
+  case 2: e = launch_exact_p<2>(a, grid, cfg, smem, c.stream); break;
+  case 4: e = launch_exact_p<4>(a, grid, cfg, smem, c.stream); break;
+  case 8: e = launch_exact_p<8>(a, grid, cfg, smem, c.stream); break;
+  default: e = launch_exact_p<16>(a, grid, cfg, smem, c.stream); break;
   }
   if (e != cudaSuccess) return cuda_error(e, "exact_kernel launch");
   c.launches++;
+  if (global_reduce) {
+    const int tb = 256;
+    slice_reduce_kernel<<<(unsigned)((c.nposes + tb - 1) / tb), tb, 0, c.stream>>>(a.partial, cfg.split, c.nposes,
+                                                                                 a.energies);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "slice_reduce_kernel launch");
+    c.launches++;
+  }
   return BUDE_OK;
 }
 
@@ -372,6 +402,7 @@ void destroy_context(Context *c) {
   c->energies.release();
   c->err.release();
   c->flush.release();
+  c->partial.release();
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);

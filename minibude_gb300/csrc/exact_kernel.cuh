@@ -14,33 +14,35 @@
 //                                                    protein hphb is non-zero and distdslv > 0)
 // The steric factor lies in [0, 1] as well (r >= 0), so all three are one `fma.rn.sat` each with
 // per-type-pair constants.  Those constants are folded into a per-ligand-type "slab" of protein
-// records built once per deck on the host (48 bytes per protein atom and ligand type):
-//   {px, py, pz, -1/radij,  -1/elcdst, 1 + radij/elcdst, -1/distdslv, 1 + radij/distdslv,
-//    45*c', d', 0, 0}
-// so one interaction is 3 FADD + FMUL + 2 FFMA (distance^2), one MUFU square root, 3 FFMA.SAT and
-// 3 FFMA (accumulate) -- 12 FP32 instructions against the reference's ~30 operations.
+// records built once per deck on the host (64 bytes per protein atom and ligand type; the values
+// used by the paired instructions below are stored twice):
+//   {px, px, py, py,  pz, pz, 45*c', 45*c',  d', d', -1/radij, -1/elcdst,
+//    1 + radij/elcdst, -1/distdslv, 1 + radij/distdslv, 0}
+// One interaction is 3 FADD + FMUL + 2 FFMA (distance^2), one MUFU square root, 3 FFMA.SAT and
+// 3 FFMA (accumulate): 12 FP32 operations against the reference's ~30.  Two poses share each
+// distance and accumulate instruction through the packed `f32x2` forms, so a pose pair costs
+// 9 paired + 6 saturating scalar FP32 instructions and 2 MUFU.
 //
 // Work decomposition.
 //   * each thread holds `P` poses (poses base + i*blockDim.x, i < P, strided like the reference,
 //     src/cuda/fasten.hpp:28,48,158): their transformed ligand atom and energy live in registers;
 //   * every warp walks the same (ligand atom, protein atom) sequence, so each protein record is a
-//     warp-uniform shared-memory broadcast (3 x LDS.128);
+//     warp-uniform shared-memory broadcast (4 x LDS.128);
 //   * protein records stream through a `kStages`-deep ring of shared-memory stages filled by 1-D
 //     TMA bulk copies (cp.async.bulk) that complete on mbarriers, prefetched kStages-1 ahead;
-//   * blockIdx.y selects a protein slice; when the launch has split > 1 slices, the blocks of one
-//     pose block form a thread-block cluster along y and rank 0 sums the slices' partial energies
-//     from distributed shared memory in slice order (deterministic, no global scratch).
+//   * blockIdx.y selects a protein slice.  With split > 1 slices the partial energies are summed in
+//     slice order either inside a thread-block cluster along y (rank 0 reads the other blocks'
+//     partials from distributed shared memory) or, without clusters, through a global
+//     [split][nposes] buffer that slice_reduce_kernel folds afterwards.  Both are deterministic.
 #pragma once
 #include <cooperative_groups.h>
 #include <cstdint>
 
+#include "exact_shape.h"
 #include "ptx.cuh"
 
 namespace bude {
 
-constexpr int kStages = 4;      // shared-memory ring depth
-constexpr int kRecF4 = 3;       // float4 per protein record (48 bytes)
-constexpr int kAtomAlign = 8;   // protein atoms are padded to a multiple of this (the unroll)
 constexpr float kSteric = 76.f; // 2 * HARDNESS (src/bude.h:32, serial/fasten.hpp:107)
 
 struct ExactArgs {
@@ -48,12 +50,14 @@ struct ExactArgs {
   const float4 *slab;     // ntypes x natpro_pad x kRecF4
   const float *xform;     // nposes x 12 pose transforms (row-major 3x4, 48 bytes per pose)
   float *energies;        // nposes
+  float *partial;         // split x nposes slice sums (global-reduce split), else unused
   unsigned int *err;      // bit 0: a bounded wait ran out
   long long nposes;
   int natlig;
   int natpro_pad;         // multiple of kAtomAlign
   int tile;               // atoms per stage, multiple of kAtomAlign
-  int split;              // protein slices (cluster size along y)
+  int split;              // protein slices (blockIdx.y)
+  int cluster;            // 1: slices reduced across a cluster; 0: through `partial`
   int slice;              // atoms per slice, multiple of kAtomAlign
 };
 
@@ -72,16 +76,20 @@ __global__ void __launch_bounds__(256) pose_xform_kernel(const float *__restrict
   xform[3 * i + 2] = make_float4(-sy, sx * cy, cx * cy, poses[5 * pstride + i]);
 }
 
-// Dynamic shared memory of exact_kernel<P> for a launch shape.
-__host__ __device__ inline size_t exact_smem_bytes(int P, int wgsize, int tile, int split) {
-  size_t b = (size_t)kStages * tile * kRecF4 * sizeof(float4) + kStages * sizeof(uint64_t);
-  if (split > 1) b += (size_t)P * wgsize * sizeof(float);
-  return b;
+
+// Fold the slice sums of the global-reduce split: energies[i] = 0.5 * sum_s partial[s][i], summed
+// in slice order.
+__global__ void __launch_bounds__(256) slice_reduce_kernel(const float *__restrict__ partial, int split,
+                                                           long long nposes, float *__restrict__ energies) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nposes) return;
+  float acc = partial[i];
+  for (int s = 1; s < split; ++s) acc += partial[(long long)s * nposes + i];
+  energies[i] = 0.5f * acc;
 }
 
-constexpr int kMaxThreads = 512; // launch bound: keeps the register budget at 128 per thread
-
-template <int P>
+// P poses per thread; U protein atoms per unrolled inner-loop body.
+template <int P, int U>
 __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   float4 *stages = reinterpret_cast<float4 *>(smem);
@@ -121,9 +129,13 @@ __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
   if (tid == 0)
     for (int q = 0; q < min(kStages - 1, Q); ++q) issue(q);
 
-  float e[P], lx[P], ly[P], lz[P];
+  // Poses are processed in pairs (i = 2j, 2j+1) so the distance and accumulate steps use the
+  // packed f32x2 instructions; with P == 1 the second lane duplicates the first and is dropped.
+  constexpr int NP = (P + 1) / 2;
+  float2 e[NP], lx[NP], ly[NP], lz[NP];
 #pragma unroll
-  for (int i = 0; i < P; ++i) e[i] = 0.f;
+  for (int j = 0; j < NP; ++j) e[j] = make_float2(0.f, 0.f);
+  const float2 steric2 = make_float2(kSteric, kSteric);
 
   bool failed = false;
   int q = 0;
@@ -134,16 +146,25 @@ __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
       // Transform ligand atom il for each pose (serial/fasten.hpp:66-73).
       const float4 la = __ldg(&a.ligand[il]);
 #pragma unroll
-      for (int i = 0; i < P; ++i) {
-        long long pi = base + (long long)i * nthr;
+      for (int i = 0; i < 2 * NP; ++i) {
+        long long pi = base + (long long)(i < P ? i : P - 1) * nthr;
         pi = pi < a.nposes ? pi : a.nposes - 1;
         // Re-read per ligand atom (volatile: the compiler must not keep 12*P transform values live
         // across the protein loop); the block's transforms stay in L1.
         const float4 *t = reinterpret_cast<const float4 *>(a.xform) + pi * 3;
         const float4 r0 = ldg_stream(t + 0), r1 = ldg_stream(t + 1), r2 = ldg_stream(t + 2);
-        lx[i] = r0.w + la.x * r0.x + la.y * r0.y + la.z * r0.z;
-        ly[i] = r1.w + la.x * r1.x + la.y * r1.y + la.z * r1.z;
-        lz[i] = r2.w + la.x * r2.x + la.y * r2.y + la.z * r2.z;
+        const float x = r0.w + la.x * r0.x + la.y * r0.y + la.z * r0.z;
+        const float y = r1.w + la.x * r1.x + la.y * r1.y + la.z * r1.z;
+        const float z = r2.w + la.x * r2.x + la.y * r2.y + la.z * r2.z;
+        if (i & 1) {
+          lx[i / 2].y = x;
+          ly[i / 2].y = y;
+          lz[i / 2].y = z;
+        } else {
+          lx[i / 2].x = x;
+          ly[i / 2].x = y;
+          lz[i / 2].x = z;
+        }
       }
     }
     // Everyone is done with step q-1, so its stage may be refilled; agree on failure first.
@@ -156,31 +177,32 @@ __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
     }
     const float4 *sp = stages + (size_t)s * a.tile * kRecF4;
     const int cnt = min(a.tile, a1 - (a0 + k * a.tile));
-    // Unroll over U atoms so one unrolled body holds about 16 interactions per thread: enough
-    // independent work to hide latency without the compiler hoisting every record into registers.
-    constexpr int U = P >= 16 ? 1 : (16 / P > kAtomAlign ? kAtomAlign : 16 / P);
+    static_assert(kAtomAlign % U == 0, "the unroll must divide the atom padding");
 #pragma unroll 1
-    for (int j = 0; j < cnt; j += U) {
+    for (int j0 = 0; j0 < cnt; j0 += U) {
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const float4 A = sp[(j + u) * kRecF4 + 0]; // px py pz -1/radij
-        const float4 B = sp[(j + u) * kRecF4 + 1]; // -1/elcdst b_chrg -1/distdslv b_dslv
-        const float4 C = sp[(j + u) * kRecF4 + 2]; // k_chrg k_dslv
+        const float4 A = sp[(j0 + u) * kRecF4 + 0]; // px px py py
+        const float4 B = sp[(j0 + u) * kRecF4 + 1]; // pz pz k_chrg k_chrg
+        const float4 C = sp[(j0 + u) * kRecF4 + 2]; // k_dslv k_dslv -1/radij -1/elcdst
+        const float4 D = sp[(j0 + u) * kRecF4 + 3]; // b_chrg -1/distdslv b_dslv 0
+        const float2 px = make_float2(A.x, A.y), py = make_float2(A.z, A.w), pz = make_float2(B.x, B.y);
+        const float2 kc = make_float2(B.z, B.w), kd = make_float2(C.x, C.y);
 #pragma unroll
-        for (int i = 0; i < P; ++i) {
-          const float dx = lx[i] - A.x;
-          const float dy = ly[i] - A.y;
-          const float dz = lz[i] - A.z;
-          float d2 = dx * dx;
-          d2 = fmaf(dy, dy, d2);
-          d2 = fmaf(dz, dz, d2);
-          const float r = sqrt_approx(d2);
-          const float fs = fma_sat(r, A.w, 1.f);
-          const float fc = fma_sat(r, B.x, B.y);
-          const float fd = fma_sat(r, B.z, B.w);
-          e[i] = fmaf(fs, kSteric, e[i]);
-          e[i] = fmaf(fc, C.x, e[i]);
-          e[i] = fmaf(fd, C.y, e[i]);
+        for (int j = 0; j < NP; ++j) {
+          const float2 dx = sub2(lx[j], px);
+          const float2 dy = sub2(ly[j], py);
+          const float2 dz = sub2(lz[j], pz);
+          float2 d2 = mul2(dx, dx);
+          d2 = fma2(dy, dy, d2);
+          d2 = fma2(dz, dz, d2);
+          const float2 r = make_float2(sqrt_approx(d2.x), sqrt_approx(d2.y));
+          const float2 fs = make_float2(fma_sat(r.x, C.z, 1.f), fma_sat(r.y, C.z, 1.f));
+          const float2 fc = make_float2(fma_sat(r.x, C.w, D.x), fma_sat(r.y, C.w, D.x));
+          const float2 fd = make_float2(fma_sat(r.x, D.y, D.z), fma_sat(r.y, D.y, D.z));
+          e[j] = fma2(fs, steric2, e[j]);
+          e[j] = fma2(fc, kc, e[j]);
+          e[j] = fma2(fd, kd, e[j]);
         }
       }
     }
@@ -196,12 +218,24 @@ __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
       (void)mbar_wait_bounded(&full[d % kStages], (uint32_t)(d / kStages) & 1u);
   }
 
+  auto energy = [&](int i) { return (i & 1) ? e[i / 2].y : e[i / 2].x; };
   if (a.split == 1) {
     if (!ok) return;
 #pragma unroll
     for (int i = 0; i < P; ++i) {
       const long long pi = base + (long long)i * nthr;
-      if (pi < a.nposes) a.energies[pi] = 0.5f * e[i];
+      if (pi < a.nposes) a.energies[pi] = 0.5f * energy(i);
+    }
+    return;
+  }
+
+  if (!a.cluster) {
+    if (!ok) return;
+    float *out = a.partial + (long long)blockIdx.y * a.nposes;
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      const long long pi = base + (long long)i * nthr;
+      if (pi < a.nposes) out[pi] = energy(i);
     }
     return;
   }
@@ -210,7 +244,7 @@ __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
 #pragma unroll
-  for (int i = 0; i < P; ++i) red[i * nthr + tid] = e[i];
+  for (int i = 0; i < P; ++i) red[i * nthr + tid] = energy(i);
   cluster.sync();
   if (blockIdx.y == 0 && ok) {
 #pragma unroll

@@ -15,6 +15,7 @@ constexpr int kHbtypeE = 69;
 constexpr float kCnstnt = 45.0f;
 constexpr float kNpNpDist = 5.5f;
 constexpr float kNpPDist = 1.0f;
+constexpr int kRecFloats = 16; // floats per slab record (exact_kernel.cuh: kRecF4 * 4)
 
 // A growable device allocation.
 struct DevBuf {
@@ -35,9 +36,13 @@ struct Context {
   bool have_deck = false;
   int natpro = 0, natpro_pad = 0, natlig = 0, ntypes = 0;
   long long nposes = 0, pose_stride = 0;
-  DevBuf ligand, slab, poses, xform, energies, err, flush;
+  DevBuf ligand, slab, poses, xform, energies, err, flush, partial;
   int flush_gen = 0;
   long long launches = 0;
+  // autotuner cache: the deck shape it was tuned for and the pick
+  long long tuned_key[3] = {-1, -1, -1};
+  bude_launch_cfg tuned{};
+  float tuned_ms = 0.f;
 };
 
 int set_error(int code, const char *fmt, ...);
@@ -56,6 +61,9 @@ int upload_deck(Context &c, const bude_atom *protein, int natpro, const bude_ato
 int set_poses(Context &c, const bude_atom *ligand, int natlig, const float *poses, long long stride,
               long long nposes);
 int check_cfg(const Context &c, const bude_launch_cfg &cfg);
+int exact_blocks_per_sm(const bude_launch_cfg &cfg, int *out);
+int choose_split(const Context &c, bude_launch_cfg &cfg);
+int autotune(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms);
 int default_cfg(const Context &c, int ppwi, int wgsize, bude_launch_cfg &cfg);
 int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid = nullptr);
 int check_device_error(Context &c);
@@ -63,3 +71,6 @@ int flush_l2(Context &c);
 int probe_kernel_arch(int device, int *cc);
 
 } // namespace bude
+
+// The opaque handle of the C-ABI is the context itself.
+struct bude_gpu_ctx : public bude::Context {};

@@ -35,8 +35,12 @@ def _poses(p) -> np.ndarray:
     return p
 
 
-def launch_cfg(ppwi: int, wgsize: int, split: int = 1, tile: int = 64) -> BudeLaunchCfg:
-    return BudeLaunchCfg(ppwi, wgsize, split, tile)
+def launch_cfg(ppwi: int, wgsize: int, split: int = 1, tile: int = 64, unroll: int = 0,
+               cluster: int = 1) -> BudeLaunchCfg:
+    """A launch shape; unroll 0 picks the usual unroll for ppwi."""
+    if unroll == 0:
+        unroll = 1 if ppwi >= 16 else 2
+    return BudeLaunchCfg(ppwi, wgsize, split, tile, unroll, cluster)
 
 
 class GpuContext:
@@ -86,6 +90,13 @@ class GpuContext:
         cfg = BudeLaunchCfg()
         check(self._lib.bude_gpu_default_cfg(self.handle, ppwi, wgsize, ctypes.byref(cfg)))
         return cfg
+
+    def autotune(self, max_ms: int = 400):
+        """(launch shape, predicted ms per evaluation) picked by the library's autotuner."""
+        cfg = BudeLaunchCfg()
+        ms = ctypes.c_float()
+        check(self._lib.bude_gpu_autotune(self.handle, max_ms, ctypes.byref(cfg), ctypes.byref(ms)))
+        return cfg, ms.value
 
     def run(self, cfg: BudeLaunchCfg) -> float:
         ms = ctypes.c_float()

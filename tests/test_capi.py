@@ -43,7 +43,7 @@ def test_version_and_error_text(built_library):
     rc = built_library.bude_gpu_create(0, None)
     assert rc == capi.BUDE_ERR_ARG
     assert "NULL" in capi.last_error()
-    cfg = capi.BudeLaunchCfg(8, 128, 1, 64)
+    cfg = capi.BudeLaunchCfg(8, 128, 1, 64, 1, 1)
     assert built_library.bude_gpu_run(None, ctypes.byref(cfg), None) == capi.BUDE_ERR_ARG
 
 

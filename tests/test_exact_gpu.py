@@ -43,15 +43,43 @@ def test_golden_default_shape(ctx, name):
     assert_parity(ctx.download(), refs, f64)
 
 
-SHAPES = list(itertools.product([1, 2, 4, 8, 16], [32, 128, 512], [1, 2, 8], [8, 64, 256]))
+SHAPES = list(itertools.product([1, 2, 4, 8, 16], [32, 128, 512], [1, 2, 8], [8, 64, 256], [1, 2, 4]))
 
 
-@pytest.mark.parametrize("ppwi,wgsize,split,tile", SHAPES)
-def test_small_all_shapes(ctx, ppwi, wgsize, split, tile):
+@pytest.mark.parametrize("ppwi,wgsize,split,tile,unroll", SHAPES)
+def test_small_all_shapes(ctx, ppwi, wgsize, split, tile, unroll):
     deck, refs, f64 = load_golden("small_head")
     ctx.upload(deck)
-    ctx.run(launch_cfg(ppwi, wgsize, split, tile))
+    ctx.run(launch_cfg(ppwi, wgsize, split, tile, unroll))
     assert_parity(ctx.download(), refs, f64)
+
+
+@pytest.mark.parametrize("ppwi,wgsize,split,unroll", [(8, 128, 3, 2), (16, 256, 16, 1), (4, 64, 64, 4),
+                                                      (2, 32, 5, 2), (1, 96, 7, 1)])
+def test_global_reduce_split_matches_cluster(ctx, ppwi, wgsize, split, unroll):
+    # Slices summed through the global buffer give the same bits as the in-cluster sum (same
+    # slice order), and both meet the parity bar.
+    deck, refs, f64 = load_golden("small_head")
+    ctx.upload(deck)
+    ctx.run(launch_cfg(ppwi, wgsize, split, 64, unroll, cluster=0))
+    a = ctx.download()
+    assert_parity(a, refs, f64)
+    if split <= 8:
+        ctx.run(launch_cfg(ppwi, wgsize, split, 64, unroll, cluster=1))
+        assert np.array_equal(a, ctx.download())
+
+
+@pytest.mark.parametrize("name", ["small_head", "bm2_head", "large_head"])
+def test_autotune_pick_is_correct(ctx, name):
+    deck, refs, f64 = load_golden(name)
+    ctx.upload(deck)
+    cfg, ms = ctx.autotune(max_ms=200)
+    assert ms > 0
+    ctx.run(cfg)
+    assert_parity(ctx.download(), refs, f64)
+    # cached for the same deck shape
+    cfg2, _ = ctx.autotune(max_ms=200)
+    assert cfg2.as_dict() == cfg.as_dict()
 
 
 @pytest.mark.parametrize("n", [1, 7, 31, 33, 129, 1000])
@@ -140,7 +168,8 @@ def test_errors(ctx):
     assert ei.value.code == BUDE_ERR_STATE
     ctx.upload(deck)
     for cfg in (launch_cfg(3, 128, 1, 64), launch_cfg(8, 100, 1, 64), launch_cfg(8, 128, 9, 64),
-                launch_cfg(8, 128, 1, 12), launch_cfg(8, 1024, 1, 64)):
+                launch_cfg(8, 128, 1, 12), launch_cfg(8, 1024, 1, 64), launch_cfg(8, 128, 1, 64, 3),
+                launch_cfg(8, 128, 65, 64, 2, 0), launch_cfg(8, 128, 2, 64, 2, 2)):
         with pytest.raises(BudeError) as ei:
             ctx.run(cfg)
         assert ei.value.code == BUDE_ERR_ARG
