@@ -18,20 +18,21 @@
 #include "../../include/minibude_gb300.h"
 #include "exact_kernel.cuh"
 #include "internal.h"
+#include "pair_record.h"
 
 namespace bude {
 
 // ---------------------------------------------------------------------------------------------
-// Errors
-static thread_local std::string g_last_error;
+// Errors: the text lives in a fixed per-thread buffer, so reporting an error never allocates.
+static thread_local char g_last_error[512];
 
 int set_error(int code, const char *fmt, ...) {
-  char buf[512];
+  char buf[sizeof g_last_error];
   va_list ap;
   va_start(ap, fmt);
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
-  g_last_error = buf;
+  std::memcpy(g_last_error, buf, sizeof buf);
   return code;
 }
 
@@ -39,51 +40,9 @@ int cuda_error(cudaError_t e, const char *what) {
   return set_error(BUDE_ERR_CUDA, "%s: %s: %s", what, cudaGetErrorName(e), cudaGetErrorString(e));
 }
 
-const char *last_error() { return g_last_error.c_str(); }
+const char *last_error() { return g_last_error; }
 
 // ---------------------------------------------------------------------------------------------
-// Pair constants (reference pair set-up, src/serial/fasten.hpp:80-96 and src/bude.h:22-35).
-// Each record feeds the three saturating FMAs of exact_kernel; the derived constants are evaluated
-// in double and rounded once, which is at least as close to the reference's FP32 expressions as
-// any FP32 evaluation order.
-void pair_record(const bude_ffparams &L, const bude_ffparams &Pp, float px, float py, float pz, float *rec) {
-  const float radij = Pp.radius + L.radius; // FP32 sum, as the reference
-  const bool both_f = Pp.hbtype == kHbtypeF && L.hbtype == kHbtypeF;
-  const double elcdst1 = both_f ? 0.25 : 0.5;
-  const bool type_e = Pp.hbtype == kHbtypeE || L.hbtype == kHbtypeE;
-  const bool p_ltz = Pp.hphb < 0.f, p_gtz = Pp.hphb > 0.f, p_nz = Pp.hphb != 0.f;
-  const bool l_ltz = L.hphb < 0.f, l_gtz = L.hphb > 0.f;
-  const float p_hphb = Pp.hphb * ((p_ltz && l_gtz) ? -1.f : 1.f);
-  const float l_hphb = L.hphb * ((p_gtz && l_ltz) ? -1.f : 1.f);
-  const float distdslv = p_ltz ? (l_ltz ? kNpNpDist : kNpPDist) : (l_ltz ? kNpPDist : -FLT_MAX);
-  const bool dslv_on = p_nz && distdslv > 0.f; // -FLT_MAX distance: the term can never fire
-  const double r_distdslv = dslv_on ? 1.0 / (double)distdslv : 1.0;
-  const float chrg_init = L.elsc * Pp.elsc;
-  const float dslv_init = p_hphb + l_hphb;
-  const float k_chrg = kCnstnt * (type_e ? -std::fabs(chrg_init) : chrg_init);
-  const float k_dslv = dslv_on ? dslv_init : 0.f;
-  rec[0] = rec[1] = px;
-  rec[2] = rec[3] = py;
-  rec[4] = rec[5] = pz;
-  rec[6] = rec[7] = k_chrg;
-  rec[8] = rec[9] = k_dslv;
-  rec[10] = (float)(-1.0 / (double)radij);
-  rec[11] = (float)(-elcdst1);
-  rec[12] = (float)(1.0 + (double)radij * elcdst1);
-  rec[13] = (float)(-r_distdslv);
-  rec[14] = dslv_on ? (float)(1.0 + (double)radij * r_distdslv) : 0.f;
-  rec[15] = 0.f;
-}
-
-// A padding atom: far away (every saturating factor is 0) with zero charge/desolvation weights.
-void null_record(float *rec) {
-  const float far = 1.0e15f;
-  for (int i = 0; i < 6; ++i) rec[i] = far;
-  for (int i = 6; i < 10; ++i) rec[i] = 0.f;
-  rec[10] = rec[11] = rec[13] = -1.f;
-  rec[12] = rec[14] = rec[15] = 0.f;
-}
-
 // slab[t][j] = record for ligand type t against protein atom j; rows padded to natpro_pad.
 void build_slab(const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes, int natpro_pad,
                 std::vector<float> &slab) {

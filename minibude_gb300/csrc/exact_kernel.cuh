@@ -43,7 +43,7 @@
 
 namespace bude {
 
-constexpr float kSteric = 76.f; // 2 * HARDNESS (src/bude.h:32, serial/fasten.hpp:107)
+constexpr float kSteric = 76.f; // 2 * HARDNESS (src/bude.h:33, serial/fasten.hpp:107)
 
 struct ExactArgs {
   const float4 *ligand;   // natlig x {x, y, z, __int_as_float(type)}
@@ -63,7 +63,8 @@ struct ExactArgs {
 
 // Pose transforms: src/cuda/fasten.hpp:45-71 / serial/fasten.hpp:28-53, one thread per pose.
 // Output: three float4 rows per pose, {r00, r01, r02, tx}, {r10, r11, r12, ty}, {r20, r21, r22, tz}.
-__global__ void __launch_bounds__(256) pose_xform_kernel(const float *__restrict__ poses, long long pstride,
+// (Internal linkage, like slice_reduce_kernel, so several translation units may include this file.)
+static __global__ void __launch_bounds__(256) pose_xform_kernel(const float *__restrict__ poses, long long pstride,
                                                          long long nposes, float4 *__restrict__ xform) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nposes) return;
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(256) pose_xform_kernel(const float *__restrict
 
 // Fold the slice sums of the global-reduce split: energies[i] = 0.5 * sum_s partial[s][i], summed
 // in slice order.
-__global__ void __launch_bounds__(256) slice_reduce_kernel(const float *__restrict__ partial, int split,
+static __global__ void __launch_bounds__(256) slice_reduce_kernel(const float *__restrict__ partial, int split,
                                                            long long nposes, float *__restrict__ energies) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nposes) return;

@@ -9,13 +9,6 @@
 
 namespace bude {
 
-// Reference constants used by the host-side pair set-up (src/bude.h:22-35).
-constexpr int kHbtypeF = 70;
-constexpr int kHbtypeE = 69;
-constexpr float kCnstnt = 45.0f;
-constexpr float kNpNpDist = 5.5f;
-constexpr float kNpPDist = 1.0f;
-constexpr int kRecFloats = 16; // floats per slab record (exact_kernel.cuh: kRecF4 * 4)
 
 // A growable device allocation.
 struct DevBuf {
@@ -49,8 +42,6 @@ int set_error(int code, const char *fmt, ...);
 int cuda_error(cudaError_t e, const char *what);
 const char *last_error();
 
-void pair_record(const bude_ffparams &L, const bude_ffparams &P, float px, float py, float pz, float *rec);
-void null_record(float *rec);
 void build_slab(const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes, int natpro_pad,
                 std::vector<float> &slab);
 
