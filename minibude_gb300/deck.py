@@ -221,6 +221,23 @@ def synthetic_deck(spec: DeckSpec, seed: int = 0, nposes: Optional[int] = None) 
     return Deck(protein, ligand, ff, poses, None, n, f"<{spec.name} seed={seed}>")
 
 
+def shard_range(n: int, rank: int, world: int):
+    """[start, stop) of rank's contiguous share of n independent items (poses or ligands); shares
+    differ by at most one item and cover 0..n exactly once."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError(f"bad rank {rank} of {world}")
+    base, extra = divmod(n, world)
+    start = rank * base + min(rank, extra)
+    return start, start + base + (1 if rank < extra else 0)
+
+
+def shard_deck(deck: Deck, rank: int, world: int) -> Deck:
+    """The rank's contiguous slice of the deck's poses (and reference energies)."""
+    a, b = shard_range(deck.nposes, rank, world)
+    refs = None if deck.ref_energies is None else deck.ref_energies[a:b].copy()
+    return dataclasses.replace(deck, poses=np.ascontiguousarray(deck.poses[:, a:b]), ref_energies=refs)
+
+
 def pose_block(poses: np.ndarray) -> np.ndarray:
     """Poses as one C-contiguous float32 [6, n] block (what the C-ABI expects)."""
     return np.ascontiguousarray(poses, dtype=np.float32)
