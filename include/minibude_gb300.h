@@ -138,6 +138,27 @@ int bude_gpu_fasten(int device, int32_t ppwi, int32_t wgsize, const bude_atom *p
  * and exact kernels count one each). */
 int bude_gpu_launch_count(const bude_gpu_ctx *ctx, int64_t *count);
 
+/* One exact evaluation that allocates no device memory.  This entry point has no counterpart in
+ * the reference.  It is for callers that may not allocate GPU memory themselves: code running
+ * inside another framework whose allocator owns the device heap, plugin hosts that hand a plugin
+ * its buffers, and loops where cudaMalloc/cudaFree and their device synchronisation are not
+ * allowed.  Every pointer is a DEVICE buffer on the current device: protein, ligand (16-byte
+ * aligned) and forcefield records, poses as six float fields at poses + k*pose_stride, and the
+ * output energies[nposes].  `stream` is a cudaStream_t (NULL: the default stream); the call
+ * returns after the energies are written.  The working memory (per-deck protein slab, pose
+ * transforms, an error word) is one fixed device array inside the library of about 11 MiB, held
+ * by every GPU that loads it until the process exits: sizes above BUDE_NOALLOC_MAX_POSES poses or
+ * BUDE_NOALLOC_MAX_SLAB_RECORDS slab records (forcefield types x protein atoms rounded up to 8)
+ * are rejected with BUDE_ERR_ARG.  Calls share that array: calls whose work overlaps on one GPU
+ * race and must be serialised by the caller.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and should come before any stream capture.  Atom types
+ * outside the forcefield give BUDE_ERR_TYPE and leave energies unwritten. */
+#define BUDE_NOALLOC_MAX_POSES 65536
+#define BUDE_NOALLOC_MAX_SLAB_RECORDS 131072
+int bude_gpu_fasten_noalloc(const bude_atom *protein, int32_t natpro, const bude_atom *ligand, int32_t natlig,
+                            const bude_ffparams *forcefield, int32_t ntypes, const float *poses, int64_t pose_stride,
+                            int64_t nposes, float *energies, void *stream);
+
 /* Page-locked host buffers for callers that time host<->device copies. */
 int bude_host_alloc(size_t bytes, void **ptr);
 int bude_host_free(void *ptr);
