@@ -134,6 +134,32 @@ int bude_gpu_fasten(int device, int32_t ppwi, int32_t wgsize, const bude_atom *p
                     const float *poses, int64_t pose_stride, int64_t nposes, int32_t iterations, float *energies,
                     float *kernel_ms, float *context_ms);
 
+/* Batched ragged scoring: many ligands, each with its own atoms and poses, against one protein.
+ * No counterpart in the reference's CUDA model, which scores one ligand per run; it replaces a
+ * loop of CudaBude::fasten calls (src/cuda/fasten.hpp:250-305), one per ligand.  Ligand l owns
+ * atoms [ligand_offsets[l], ligand_offsets[l+1]) of ligand_atoms and poses
+ * [pose_offsets[l], pose_offsets[l+1]) of the [6][pose_stride] pose block; both offset arrays
+ * have nligands+1 entries starting at 0.  A batch replaces any deck uploaded to the context (and
+ * vice versa); energies come out in the concatenated pose order. */
+int bude_gpu_upload_batch(bude_gpu_ctx *ctx, const bude_atom *protein, int32_t natpro,
+                          const bude_ffparams *forcefield, int32_t ntypes, int32_t nligands,
+                          const bude_atom *ligand_atoms, const int32_t *ligand_offsets, const float *poses,
+                          int64_t pose_stride, const int64_t *pose_offsets);
+
+/* Launch shape for the batch (ppwi, wgsize, tile, unroll; split and cluster are not used): each
+ * candidate is timed on a strided subset of the batch's work items.  Cached per batch. */
+int bude_gpu_autotune_batch(bude_gpu_ctx *ctx, int32_t max_ms, bude_launch_cfg *best, float *best_ms);
+
+/* One evaluation of the whole batch, then a stream synchronise.  per_ligand = 0: one persistent
+ * kernel over all (ligand, pose block) items, longest first, taken from an atomic work counter,
+ * launched as a CUDA graph (counter reset + pose transforms + persistent kernel) captured on first
+ * use of a launch shape.  per_ligand = 1: one plain exact-kernel launch per ligand, for
+ * comparison.  *ms (optional) receives the CUDA-event time. */
+int bude_gpu_run_batch(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, int32_t per_ligand, float *ms);
+
+/* Energies of the last batch evaluation, in concatenated pose order. */
+int bude_gpu_download_batch(bude_gpu_ctx *ctx, float *energies, int64_t total_poses);
+
 /* Number of kernels this library launched on the context since it was created (the transform
  * and exact kernels count one each). */
 int bude_gpu_launch_count(const bude_gpu_ctx *ctx, int64_t *count);

@@ -72,6 +72,10 @@ SIGNATURES = [
                                            c_float_p]),
     ("bude_gpu_fasten", ctypes.c_int, [ctypes.c_int, c_int32, c_int32, _P, c_int32, _P, c_int32, _P, c_int32, _P,
                                        c_int64, c_int64, c_int32, c_float_p, c_float_p, c_float_p]),
+    ("bude_gpu_upload_batch", ctypes.c_int, [_P, _P, c_int32, _P, c_int32, c_int32, _P, _P, _P, c_int64, _P]),
+    ("bude_gpu_autotune_batch", ctypes.c_int, [_P, c_int32, ctypes.POINTER(BudeLaunchCfg), c_float_p]),
+    ("bude_gpu_run_batch", ctypes.c_int, [_P, ctypes.POINTER(BudeLaunchCfg), c_int32, c_float_p]),
+    ("bude_gpu_download_batch", ctypes.c_int, [_P, c_float_p, c_int64]),
     ("bude_gpu_launch_count", ctypes.c_int, [_P, ctypes.POINTER(c_int64)]),
     ("bude_gpu_fasten_noalloc", ctypes.c_int, [_P, c_int32, _P, c_int32, _P, c_int32, _P, c_int64, c_int64, _P, _P]),
     ("bude_host_alloc", ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),

@@ -32,15 +32,19 @@ static int ppwi_to_p(int ppwi) {
 // (rounds = ceil(blocks * S / slots); the small per-slice term covers the reduction and the
 // shorter protein loop of thin slices).  Slices keep at least 64 protein atoms.
 int choose_split(const Context &c, bude_launch_cfg &cfg) {
+  return choose_split_for(c.num_sms, c.natpro_pad, c.nposes, cfg);
+}
+
+int choose_split_for(int num_sms, int natpro_pad, long long nposes, bude_launch_cfg &cfg) {
   cfg.split = 1;
   int per_sm = 0;
   int rc = exact_blocks_per_sm(cfg, &per_sm);
   if (rc) return rc;
   if (per_sm <= 0) return set_error(BUDE_ERR_ARG, "launch shape cannot be resident on an SM");
-  const long long slots = (long long)per_sm * std::max(c.num_sms, 1);
+  const long long slots = (long long)per_sm * std::max(num_sms, 1);
   const long long ppb = (long long)cfg.ppwi * cfg.wgsize;
-  const long long blocks = std::max<long long>(1, (c.nposes + ppb - 1) / ppb);
-  const int smax = std::max(1, std::min(cfg.cluster ? 8 : 64, c.natpro_pad / 64));
+  const long long blocks = std::max<long long>(1, (nposes + ppb - 1) / ppb);
+  const int smax = std::max(1, std::min(cfg.cluster ? 8 : 64, natpro_pad / 64));
   double best = 1e300;
   for (int s = 1; s <= smax; ++s) {
     const long long rounds = (blocks * s + slots - 1) / slots;

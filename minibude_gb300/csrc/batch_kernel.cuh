@@ -1,0 +1,111 @@
+// batch_kernel.cuh -- persistent exact scoring of many ligands, each with its own poses.
+//
+// The work of a batch (ligand l has natlig_l atoms and nposes_l poses, all against one protein)
+// is cut into items of one pose block each: (first ligand atom, natlig, first pose, pose count),
+// with at most P * blockDim poses per item.  The host orders items longest first (natlig
+// descending).  A grid of exactly the resident block slots loops: one thread takes the next item
+// from a global counter (atomicAdd), the block scores it with the exact kernel's arithmetic
+// (PosePairs::transform / tile, exact_kernel.cuh) over the whole protein, writes 0.5 * etot for
+// its poses and takes the next item.  The shared-memory ring and its mbarrier phases run on across
+// items (a global step counter), so no barrier is re-initialised.
+#pragma once
+#include "exact_kernel.cuh"
+
+namespace bude {
+
+struct BatchArgs {
+  const float4 *ligands; // all ligands' atoms: {x, y, z, __int_as_float(type)}
+  const float4 *slab;    // ntypes x natpro_pad x kRecF4
+  const float *xform;    // total poses x 12
+  float *energies;       // total poses
+  const int4 *items;     // {first ligand atom, natlig, first pose, pose count}
+  unsigned int *counter; // next item; zero before the launch
+  unsigned int *err;     // bit 0: a bounded wait ran out
+  int n_items;
+  int natpro_pad;
+  int tile;
+};
+
+template <int P, int U>
+__global__ void __launch_bounds__(kMaxThreads) batch_kernel(const BatchArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  float4 *stages = reinterpret_cast<float4 *>(smem);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)kStages * a.tile * kRecF4 * sizeof(float4));
+  __shared__ int s_item;
+
+  const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
+  const int ntile = (a.natpro_pad + a.tile - 1) / a.tile;
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  long long qg = 0; // steps already run by this block (stage = step % kStages, phase from step / kStages)
+  bool failed = false;
+  for (;;) {
+    if (tid == 0) s_item = (int)atomicAdd(a.counter, 1u);
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads(); // s_item is rewritten only after every thread has read it
+    if (item >= a.n_items) break;
+    const int4 it = __ldg(&a.items[item]);
+    const float4 *lig = a.ligands + it.x;
+    const int Q = it.y * ntile;
+    const long long base = (long long)it.z + tid;
+    const long long end = (long long)it.z + it.w;
+
+    auto issue = [&](int q) {
+      const int il = q / ntile;
+      const int k = q - il * ntile;
+      const int lt = __float_as_int(__ldg(&lig[il]).w);
+      const int first = k * a.tile;
+      const int cnt = min(a.tile, a.natpro_pad - first);
+      const int s = (int)((qg + q) % kStages);
+      const uint32_t bytes = (uint32_t)cnt * kRecF4 * sizeof(float4);
+      mbar_arrive_expect_tx(&full[s], bytes);
+      bulk_g2s(stages + (size_t)s * a.tile * kRecF4, a.slab + ((size_t)lt * a.natpro_pad + first) * kRecF4, bytes,
+               &full[s]);
+    };
+    if (tid == 0)
+      for (int q = 0; q < min(kStages - 1, Q); ++q) issue(q);
+
+    PosePairs<P> pp;
+    pp.clear();
+    int q = 0;
+    for (; q < Q; ++q) {
+      const int il = q / ntile;
+      const int k = q - il * ntile;
+      if (k == 0) pp.transform(__ldg(&lig[il]), a.xform, base, nthr, end);
+      if (__syncthreads_or(failed)) break;
+      if (tid == 0 && q + kStages - 1 < Q) issue(q + kStages - 1);
+      const long long step = qg + q;
+      const int s = (int)(step % kStages);
+      if (!mbar_wait_bounded(&full[s], (uint32_t)(step / kStages) & 1u)) {
+        failed = true;
+        continue;
+      }
+      pp.template tile<U>(stages + (size_t)s * a.tile * kRecF4, min(a.tile, a.natpro_pad - k * a.tile));
+    }
+    const bool ok = !__syncthreads_or(failed || q < Q);
+    if (!ok) {
+      if (tid == 0) {
+        // Record the timeout and wait (bounded) for this block's copies still in flight.
+        atomicOr(a.err, 1u);
+        for (int d = max(0, q - 1); d < min(Q, q + kStages - 1); ++d)
+          (void)mbar_wait_bounded(&full[(qg + d) % kStages], (uint32_t)((qg + d) / kStages) & 1u);
+      }
+      return;
+    }
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      const long long pi = base + (long long)i * nthr;
+      if (pi < end) a.energies[pi] = 0.5f * pp.energy(i);
+    }
+    qg += Q;
+  }
+}
+
+} // namespace bude

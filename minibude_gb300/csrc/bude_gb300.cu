@@ -185,15 +185,24 @@ int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid) {
     c.launches++;
   }
   if (mid) cudaEventRecord(mid, c.stream);
+  return launch_exact_range(c, cfg, c.ligand.as<float4>(), c.natlig, c.xform.as<float>(), c.energies.as<float>(),
+                            c.nposes);
+}
+
+// The exact kernel (and, for a global-reduce split, slice_reduce_kernel) over `nposes` poses whose
+// transforms are at `xform`, for the ligand at `ligand`; energies land at `energies`.
+int launch_exact_range(Context &c, const bude_launch_cfg &cfg, const float4 *ligand, int natlig, const float *xform,
+                       float *energies, long long nposes) {
+  if (nposes == 0) return BUDE_OK;
   ExactArgs a;
-  a.ligand = c.ligand.as<float4>();
+  a.ligand = ligand;
   a.slab = c.slab.as<float4>();
-  a.xform = c.xform.as<float>();
-  a.energies = c.energies.as<float>();
+  a.xform = xform;
+  a.energies = energies;
   a.partial = nullptr;
   a.err = c.err.as<unsigned int>();
-  a.nposes = c.nposes;
-  a.natlig = c.natlig;
+  a.nposes = nposes;
+  a.natlig = natlig;
   a.natpro_pad = c.natpro_pad;
   a.tile = cfg.tile;
   a.split = cfg.split;
@@ -201,13 +210,13 @@ int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid) {
   const bool global_reduce = cfg.split > 1 && !cfg.cluster;
   if (global_reduce) {
     // Slice sums go through a [split][nposes] buffer owned by the context.
-    int rc2 = c.partial.reserve((size_t)cfg.split * c.nposes * sizeof(float), "slice partial sums");
+    int rc2 = c.partial.reserve((size_t)cfg.split * nposes * sizeof(float), "slice partial sums");
     if (rc2) return rc2;
     a.partial = c.partial.as<float>();
   }
   a.slice = round_up((c.natpro_pad + cfg.split - 1) / cfg.split, kAtomAlign);
   const long long ppb = (long long)cfg.ppwi * cfg.wgsize;
-  const long long nbx = (c.nposes + ppb - 1) / ppb;
+  const long long nbx = (nposes + ppb - 1) / ppb;
   if (nbx > 0x7fffffffLL) return set_error(BUDE_ERR_ARG, "too many poses for one launch");
   dim3 grid((unsigned)nbx, (unsigned)cfg.split, 1);
   const size_t smem = exact_smem_bytes(cfg.ppwi, cfg.wgsize, cfg.tile, cfg.split, cfg.cluster);
@@ -223,8 +232,8 @@ int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid) {
   c.launches++;
   if (global_reduce) {
     const int tb = 256;
-    slice_reduce_kernel<<<(unsigned)((c.nposes + tb - 1) / tb), tb, 0, c.stream>>>(a.partial, cfg.split, c.nposes,
-                                                                                 a.energies);
+    slice_reduce_kernel<<<(unsigned)((nposes + tb - 1) / tb), tb, 0, c.stream>>>(a.partial, cfg.split, nposes,
+                                                                               a.energies);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "slice_reduce_kernel launch");
     c.launches++;
@@ -283,6 +292,7 @@ static int upload_poses(Context &c, const float *poses, long long stride, long l
 int upload_deck(Context &c, const bude_atom *protein, int natpro, const bude_atom *ligand, int natlig,
                 const bude_ffparams *ff, int ntypes, const float *poses, long long stride, long long nposes) {
   c.have_deck = false; // a failed upload leaves no deck behind
+  c.have_batch = false; // the slab now belongs to this deck
   if (natpro < 0 || natlig < 0 || ntypes <= 0 || !ff || (natpro > 0 && !protein) || (natlig > 0 && !ligand))
     return set_error(BUDE_ERR_ARG, "bad deck sizes or pointers (natpro %d, natlig %d, ntypes %d)", natpro, natlig,
                      ntypes);
@@ -362,6 +372,7 @@ void destroy_context(Context *c) {
   c->err.release();
   c->flush.release();
   c->partial.release();
+  release_batch(*c);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);

@@ -89,6 +89,81 @@ static __global__ void __launch_bounds__(256) slice_reduce_kernel(const float *_
   energies[i] = 0.5f * acc;
 }
 
+// Poses are processed in pairs (i = 2j, 2j+1) so the distance and accumulate steps use the packed
+// f32x2 instructions; with P == 1 the second lane duplicates the first and is dropped.
+template <int P> struct PosePairs {
+  static constexpr int NP = (P + 1) / 2;
+  float2 e[NP], lx[NP], ly[NP], lz[NP];
+
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int j = 0; j < NP; ++j) e[j] = make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ float energy(int i) const { return (i & 1) ? e[i / 2].y : e[i / 2].x; }
+
+  // Transform ligand atom `la` for the thread's poses base + i*stride (serial/fasten.hpp:66-73);
+  // pose indices at or past `end` read pose end-1 instead.  The transforms are re-read per ligand
+  // atom (volatile loads: the compiler must not keep 12*P values live across the protein loop);
+  // a block's transforms stay in L1.
+  __device__ __forceinline__ void transform(float4 la, const float *xform, long long base, int stride,
+                                            long long end) {
+#pragma unroll
+    for (int i = 0; i < 2 * NP; ++i) {
+      long long pi = base + (long long)(i < P ? i : P - 1) * stride;
+      pi = pi < end ? pi : end - 1;
+      const float4 *t = reinterpret_cast<const float4 *>(xform) + pi * 3;
+      const float4 r0 = ldg_stream(t + 0), r1 = ldg_stream(t + 1), r2 = ldg_stream(t + 2);
+      const float x = r0.w + la.x * r0.x + la.y * r0.y + la.z * r0.z;
+      const float y = r1.w + la.x * r1.x + la.y * r1.y + la.z * r1.z;
+      const float z = r2.w + la.x * r2.x + la.y * r2.y + la.z * r2.z;
+      if (i & 1) {
+        lx[i / 2].y = x;
+        ly[i / 2].y = y;
+        lz[i / 2].y = z;
+      } else {
+        lx[i / 2].x = x;
+        ly[i / 2].x = y;
+        lz[i / 2].x = z;
+      }
+    }
+  }
+
+  // Accumulate the interactions with `cnt` protein records staged at `sp` (cnt a multiple of U):
+  // the restated pair energy of the file comment, src/serial/fasten.hpp:98-124.
+  template <int U> __device__ __forceinline__ void tile(const float4 *sp, int cnt) {
+    static_assert(kAtomAlign % U == 0, "the unroll must divide the atom padding");
+    const float2 steric2 = make_float2(kSteric, kSteric);
+#pragma unroll 1
+    for (int j0 = 0; j0 < cnt; j0 += U) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float4 A = sp[(j0 + u) * kRecF4 + 0]; // px px py py
+        const float4 B = sp[(j0 + u) * kRecF4 + 1]; // pz pz k_chrg k_chrg
+        const float4 C = sp[(j0 + u) * kRecF4 + 2]; // k_dslv k_dslv -1/radij -1/elcdst
+        const float4 D = sp[(j0 + u) * kRecF4 + 3]; // b_chrg -1/distdslv b_dslv 0
+        const float2 px = make_float2(A.x, A.y), py = make_float2(A.z, A.w), pz = make_float2(B.x, B.y);
+        const float2 kc = make_float2(B.z, B.w), kd = make_float2(C.x, C.y);
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+          const float2 dx = sub2(lx[j], px);
+          const float2 dy = sub2(ly[j], py);
+          const float2 dz = sub2(lz[j], pz);
+          float2 d2 = mul2(dx, dx);
+          d2 = fma2(dy, dy, d2);
+          d2 = fma2(dz, dz, d2);
+          const float2 r = make_float2(sqrt_approx(d2.x), sqrt_approx(d2.y));
+          const float2 fs = make_float2(fma_sat(r.x, C.z, 1.f), fma_sat(r.y, C.z, 1.f));
+          const float2 fc = make_float2(fma_sat(r.x, C.w, D.x), fma_sat(r.y, C.w, D.x));
+          const float2 fd = make_float2(fma_sat(r.x, D.y, D.z), fma_sat(r.y, D.y, D.z));
+          e[j] = fma2(fs, steric2, e[j]);
+          e[j] = fma2(fc, kc, e[j]);
+          e[j] = fma2(fd, kd, e[j]);
+        }
+      }
+    }
+  }
+};
+
 // P poses per thread; U protein atoms per unrolled inner-loop body.
 template <int P, int U>
 __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
@@ -130,44 +205,15 @@ __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
   if (tid == 0)
     for (int q = 0; q < min(kStages - 1, Q); ++q) issue(q);
 
-  // Poses are processed in pairs (i = 2j, 2j+1) so the distance and accumulate steps use the
-  // packed f32x2 instructions; with P == 1 the second lane duplicates the first and is dropped.
-  constexpr int NP = (P + 1) / 2;
-  float2 e[NP], lx[NP], ly[NP], lz[NP];
-#pragma unroll
-  for (int j = 0; j < NP; ++j) e[j] = make_float2(0.f, 0.f);
-  const float2 steric2 = make_float2(kSteric, kSteric);
+  PosePairs<P> pp;
+  pp.clear();
 
   bool failed = false;
   int q = 0;
   for (; q < Q; ++q) {
     const int il = q / ntile;
     const int k = q - il * ntile;
-    if (k == 0) {
-      // Transform ligand atom il for each pose (serial/fasten.hpp:66-73).
-      const float4 la = __ldg(&a.ligand[il]);
-#pragma unroll
-      for (int i = 0; i < 2 * NP; ++i) {
-        long long pi = base + (long long)(i < P ? i : P - 1) * nthr;
-        pi = pi < a.nposes ? pi : a.nposes - 1;
-        // Re-read per ligand atom (volatile: the compiler must not keep 12*P transform values live
-        // across the protein loop); the block's transforms stay in L1.
-        const float4 *t = reinterpret_cast<const float4 *>(a.xform) + pi * 3;
-        const float4 r0 = ldg_stream(t + 0), r1 = ldg_stream(t + 1), r2 = ldg_stream(t + 2);
-        const float x = r0.w + la.x * r0.x + la.y * r0.y + la.z * r0.z;
-        const float y = r1.w + la.x * r1.x + la.y * r1.y + la.z * r1.z;
-        const float z = r2.w + la.x * r2.x + la.y * r2.y + la.z * r2.z;
-        if (i & 1) {
-          lx[i / 2].y = x;
-          ly[i / 2].y = y;
-          lz[i / 2].y = z;
-        } else {
-          lx[i / 2].x = x;
-          ly[i / 2].x = y;
-          lz[i / 2].x = z;
-        }
-      }
-    }
+    if (k == 0) pp.transform(__ldg(&a.ligand[il]), a.xform, base, nthr, a.nposes);
     // Everyone is done with step q-1, so its stage may be refilled; agree on failure first.
     if (__syncthreads_or(failed)) break;
     if (tid == 0 && q + kStages - 1 < Q) issue(q + kStages - 1);
@@ -176,37 +222,7 @@ __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
       failed = true;
       continue;
     }
-    const float4 *sp = stages + (size_t)s * a.tile * kRecF4;
-    const int cnt = min(a.tile, a1 - (a0 + k * a.tile));
-    static_assert(kAtomAlign % U == 0, "the unroll must divide the atom padding");
-#pragma unroll 1
-    for (int j0 = 0; j0 < cnt; j0 += U) {
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const float4 A = sp[(j0 + u) * kRecF4 + 0]; // px px py py
-        const float4 B = sp[(j0 + u) * kRecF4 + 1]; // pz pz k_chrg k_chrg
-        const float4 C = sp[(j0 + u) * kRecF4 + 2]; // k_dslv k_dslv -1/radij -1/elcdst
-        const float4 D = sp[(j0 + u) * kRecF4 + 3]; // b_chrg -1/distdslv b_dslv 0
-        const float2 px = make_float2(A.x, A.y), py = make_float2(A.z, A.w), pz = make_float2(B.x, B.y);
-        const float2 kc = make_float2(B.z, B.w), kd = make_float2(C.x, C.y);
-#pragma unroll
-        for (int j = 0; j < NP; ++j) {
-          const float2 dx = sub2(lx[j], px);
-          const float2 dy = sub2(ly[j], py);
-          const float2 dz = sub2(lz[j], pz);
-          float2 d2 = mul2(dx, dx);
-          d2 = fma2(dy, dy, d2);
-          d2 = fma2(dz, dz, d2);
-          const float2 r = make_float2(sqrt_approx(d2.x), sqrt_approx(d2.y));
-          const float2 fs = make_float2(fma_sat(r.x, C.z, 1.f), fma_sat(r.y, C.z, 1.f));
-          const float2 fc = make_float2(fma_sat(r.x, C.w, D.x), fma_sat(r.y, C.w, D.x));
-          const float2 fd = make_float2(fma_sat(r.x, D.y, D.z), fma_sat(r.y, D.y, D.z));
-          e[j] = fma2(fs, steric2, e[j]);
-          e[j] = fma2(fc, kc, e[j]);
-          e[j] = fma2(fd, kd, e[j]);
-        }
-      }
-    }
+    pp.template tile<U>(stages + (size_t)s * a.tile * kRecF4, min(a.tile, a1 - (a0 + k * a.tile)));
   }
 
   // A wait that ran out on any thread (including in the last step) fails the whole block.
@@ -219,7 +235,7 @@ __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
       (void)mbar_wait_bounded(&full[d % kStages], (uint32_t)(d / kStages) & 1u);
   }
 
-  auto energy = [&](int i) { return (i & 1) ? e[i / 2].y : e[i / 2].x; };
+  auto energy = [&](int i) { return pp.energy(i); };
   if (a.split == 1) {
     if (!ok) return;
 #pragma unroll

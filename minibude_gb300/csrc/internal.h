@@ -32,6 +32,20 @@ struct Context {
   DevBuf ligand, slab, poses, xform, energies, err, flush, partial;
   int flush_gen = 0;
   long long launches = 0;
+  // batch of ligands (bude_gpu_upload_batch); shares the protein slab with the deck fields above
+  bool have_batch = false;
+  int nligands = 0;
+  std::vector<int> lig_off;        // nligands + 1 atom offsets
+  std::vector<long long> pose_off; // nligands + 1 pose offsets
+  long long batch_poses = 0;
+  DevBuf b_ligands, b_poses, b_xform, b_energies, b_items, b_counter;
+  int items_ppb = 0; // poses per item the device item list was built for
+  int n_items = 0;
+  cudaGraphExec_t graph = nullptr;
+  bude_launch_cfg graph_cfg{};
+  long long batch_tuned_key = -1;
+  bude_launch_cfg batch_tuned{};
+  float batch_tuned_ms = 0.f;
   // autotuner cache: the deck shape it was tuned for and the pick
   long long tuned_key[3] = {-1, -1, -1};
   bude_launch_cfg tuned{};
@@ -54,9 +68,13 @@ int set_poses(Context &c, const bude_atom *ligand, int natlig, const float *pose
 int check_cfg(const Context &c, const bude_launch_cfg &cfg);
 int exact_blocks_per_sm(const bude_launch_cfg &cfg, int *out);
 int choose_split(const Context &c, bude_launch_cfg &cfg);
+int choose_split_for(int num_sms, int natpro_pad, long long nposes, bude_launch_cfg &cfg);
+void release_batch(Context &c);
 int autotune(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms);
 int default_cfg(const Context &c, int ppwi, int wgsize, bude_launch_cfg &cfg);
 int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid = nullptr);
+int launch_exact_range(Context &c, const bude_launch_cfg &cfg, const float4 *ligand, int natlig, const float *xform,
+                       float *energies, long long nposes);
 int check_device_error(Context &c);
 int flush_l2(Context &c);
 int probe_kernel_arch(int device, int *cc);

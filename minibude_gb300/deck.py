@@ -221,6 +221,96 @@ def synthetic_deck(spec: DeckSpec, seed: int = 0, nposes: Optional[int] = None) 
     return Deck(protein, ligand, ff, poses, None, n, f"<{spec.name} seed={seed}>")
 
 
+@dataclasses.dataclass
+class BatchDeck:
+    """Many ligands, each with its own atoms and poses, against one protein."""
+    protein: np.ndarray  # ATOM_DTYPE [natpro]
+    forcefield: np.ndarray  # FF_DTYPE [ntypes]
+    ligands: list  # of ATOM_DTYPE arrays
+    poses: list  # of float32 [6, n_l] arrays
+    name: str = ""
+
+    @property
+    def nligands(self) -> int:
+        return len(self.ligands)
+
+    @property
+    def natpro(self) -> int:
+        return int(self.protein.shape[0])
+
+    @property
+    def ntypes(self) -> int:
+        return int(self.forcefield.shape[0])
+
+    def ligand_offsets(self) -> np.ndarray:
+        return np.concatenate([[0], np.cumsum([len(l) for l in self.ligands])]).astype(np.int32)
+
+    def pose_offsets(self) -> np.ndarray:
+        return np.concatenate([[0], np.cumsum([p.shape[1] for p in self.poses])]).astype(np.int64)
+
+    @property
+    def total_poses(self) -> int:
+        return int(sum(p.shape[1] for p in self.poses))
+
+    @property
+    def interactions(self) -> int:
+        return int(sum(len(l) * p.shape[1] for l, p in zip(self.ligands, self.poses))) * self.natpro
+
+    def atoms(self) -> np.ndarray:
+        return concat_atoms(self.ligands)
+
+    def pose_block(self) -> np.ndarray:
+        if not self.poses:
+            return np.zeros((6, 0), np.float32)
+        return np.ascontiguousarray(np.concatenate(self.poses, axis=1), dtype=np.float32)
+
+    def deck(self, l: int) -> Deck:
+        """Ligand l as a plain deck."""
+        return Deck(self.protein, self.ligands[l], self.forcefield, np.ascontiguousarray(self.poses[l]), None,
+                    self.poses[l].shape[1], f"{self.name}[{l}]")
+
+    def subset(self, ligands, max_poses=None) -> "BatchDeck":
+        """Some of the ligands, optionally with only their first max_poses poses."""
+        return BatchDeck(self.protein, self.forcefield, [self.ligands[l] for l in ligands],
+                         [np.ascontiguousarray(self.poses[l][:, :max_poses]) for l in ligands], self.name)
+
+
+@dataclasses.dataclass(frozen=True)
+class BatchSpec:
+    """Shape of a synthetic batch: ligand atom counts uniform in [atoms_lo, atoms_hi], pose counts
+    log-uniform in [poses_lo, poses_hi] (or all equal to poses_lo when poses_hi == poses_lo)."""
+    name: str
+    nligands: int
+    atoms_lo: int
+    atoms_hi: int
+    poses_lo: int
+    poses_hi: int
+    ligand_radius: float = 5.0
+    max_trans: float = 3.0
+
+
+# 256 ligands of 12-96 atoms with 4,096-65,536 poses each (log-uniform) against one protein.
+BATCH = BatchSpec("batch-256-ligands-12to96-atoms-4096to65536-poses", 256, 12, 96, 4096, 65536)
+
+
+def synthetic_batch(spec: BatchSpec, protein: np.ndarray, forcefield: np.ndarray, seed: int = 0) -> BatchDeck:
+    """Seeded ligands (atoms uniform within ligand_radius of the origin, types uniform over the
+    forcefield) and poses (angles U[0, 2pi), translations U[-max_trans, max_trans])."""
+    rng = np.random.Generator(np.random.PCG64([seed, 2]))
+    ntypes = forcefield.shape[0]
+    ligands, poses = [], []
+    for _ in range(spec.nligands):
+        natlig = int(rng.integers(spec.atoms_lo, spec.atoms_hi + 1))
+        if spec.poses_hi > spec.poses_lo:
+            n = int(round(math.exp(rng.uniform(math.log(spec.poses_lo), math.log(spec.poses_hi)))))
+        else:
+            n = spec.poses_lo
+        ligands.append(synthetic_ligand(rng, natlig, spec.ligand_radius, ntypes))
+        poses.append(synthetic_poses(rng, n, spec.max_trans))
+    return BatchDeck(np.ascontiguousarray(protein, ATOM_DTYPE), np.ascontiguousarray(forcefield, FF_DTYPE), ligands,
+                     poses, spec.name)
+
+
 def shard_range(n: int, rank: int, world: int):
     """[start, stop) of rank's contiguous share of n independent items (poses or ligands); shares
     differ by at most one item and cover 0..n exactly once."""

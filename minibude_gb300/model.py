@@ -127,6 +127,34 @@ class GpuContext:
         self.nposes = poses.shape[1]
         return energies
 
+    # -- batches of ligands -------------------------------------------------------------------
+    def upload_batch(self, batch) -> None:
+        protein, ff = _atoms(batch.protein), _ff(batch.forcefield)
+        atoms = _atoms(batch.atoms())
+        lig_off = np.ascontiguousarray(batch.ligand_offsets(), np.int32)
+        pose_off = np.ascontiguousarray(batch.pose_offsets(), np.int64)
+        poses = _poses(batch.pose_block())
+        check(self._lib.bude_gpu_upload_batch(self.handle, ptr(protein), protein.size, ptr(ff), ff.size,
+                                              batch.nligands, ptr(atoms), ptr(lig_off), ptr(poses), poses.shape[1],
+                                              ptr(pose_off)))
+        self.batch_poses = poses.shape[1]
+
+    def autotune_batch(self, max_ms: int = 2000):
+        cfg = BudeLaunchCfg()
+        ms = ctypes.c_float()
+        check(self._lib.bude_gpu_autotune_batch(self.handle, max_ms, ctypes.byref(cfg), ctypes.byref(ms)))
+        return cfg, ms.value
+
+    def run_batch(self, cfg: BudeLaunchCfg, per_ligand: bool = False) -> float:
+        ms = ctypes.c_float()
+        check(self._lib.bude_gpu_run_batch(self.handle, ctypes.byref(cfg), int(per_ligand), ctypes.byref(ms)))
+        return ms.value
+
+    def download_batch(self) -> np.ndarray:
+        out = np.zeros(self.batch_poses, np.float32)
+        check(self._lib.bude_gpu_download_batch(self.handle, fptr(out), self.batch_poses))
+        return out
+
     def launch_count(self) -> int:
         n = ctypes.c_int64()
         check(self._lib.bude_gpu_launch_count(self.handle, ctypes.byref(n)))

@@ -1,0 +1,120 @@
+"""Batched ragged scoring (persistent CUDA-graph launch and one launch per ligand) against the oracle
+and the single-deck path."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import load_golden
+from minibude_gb300 import BatchSpec, synthetic_batch, validate
+from minibude_gb300.capi import BUDE_ERR_ARG, BUDE_ERR_STATE, BUDE_ERR_TYPE, BudeError
+from minibude_gb300.model import GpuContext, launch_cfg
+
+pytestmark = pytest.mark.gpu
+F64_TOL = 2e-4
+
+
+def bm2_protein():
+    deck, _, _ = load_golden("bm2_head")
+    return deck.protein, deck.forcefield
+
+
+def small_batch(seed=0, n=12, lo=12, hi=96, plo=50, phi=3000):
+    protein, ff = bm2_protein()
+    return synthetic_batch(BatchSpec("t", n, lo, hi, plo, phi), protein, ff, seed)
+
+
+def oracle_batch(batch):
+    e32 = np.concatenate([oracle.fasten_f32(batch.deck(l)) for l in range(batch.nligands)])
+    e64 = np.concatenate([oracle.fasten_f64(batch.deck(l)) for l in range(batch.nligands)])
+    return e32, e64
+
+
+def assert_parity(got, want, f64):
+    assert np.all(np.isfinite(got))
+    max_diff, failed = validate(got, want)
+    assert not failed and max_diff < 0.025, (max_diff, failed[:5])
+    err = np.abs(got.astype(np.float64) - f64) / np.maximum(np.abs(f64), 1.0)
+    assert err.max() < F64_TOL, err.max()
+
+
+@pytest.fixture(scope="module")
+def ctx(built_library):
+    c = GpuContext(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def batch_and_refs():
+    b = small_batch()
+    return b, oracle_batch(b)
+
+
+@pytest.mark.parametrize("ppwi,wgsize,unroll", [(16, 128, 1), (8, 128, 2), (4, 64, 4), (2, 96, 2), (1, 32, 1)])
+def test_persistent_batch_matches_oracle(ctx, batch_and_refs, ppwi, wgsize, unroll):
+    b, (e32, e64) = batch_and_refs
+    ctx.upload_batch(b)
+    ctx.run_batch(launch_cfg(ppwi, wgsize, 1, 64, unroll))
+    got = ctx.download_batch()
+    assert_parity(got, e32, e64)
+    # the captured graph is relaunched: same bits
+    ctx.run_batch(launch_cfg(ppwi, wgsize, 1, 64, unroll))
+    assert np.array_equal(got, ctx.download_batch())
+
+
+def test_persistent_equals_per_ligand_unsplit(ctx, batch_and_refs):
+    # Without a protein split every launch shape sums each pose in the same order, so the
+    # persistent kernel and one plain launch per ligand agree bit for bit.
+    b, (e32, e64) = batch_and_refs
+    ctx.upload_batch(b)
+    ctx.run_batch(launch_cfg(8, 128, 1, 64, 2))
+    persistent = ctx.download_batch()
+    per_lig = []
+    for l in range(b.nligands):
+        ctx.upload(b.deck(l))
+        ctx.run(launch_cfg(8, 128, 1, 64, 2))
+        per_lig.append(ctx.download())
+    assert np.array_equal(persistent, np.concatenate(per_lig))
+
+
+def test_per_ligand_mode_matches_oracle(ctx, batch_and_refs):
+    b, (e32, e64) = batch_and_refs
+    ctx.upload_batch(b)
+    ctx.run_batch(launch_cfg(8, 128, 1, 64, 2), per_ligand=True)
+    assert_parity(ctx.download_batch(), e32, e64)
+
+
+def test_batch_autotune_and_ragged_edges(ctx):
+    # ligands with 1 atom and 1 pose, an empty pose list and the largest sizes in one batch
+    protein, ff = bm2_protein()
+    b = synthetic_batch(BatchSpec("edge", 5, 1, 96, 1, 1), protein, ff, 3)
+    b.poses[2] = b.poses[2][:, :0]
+    b.poses[4] = synthetic_batch(BatchSpec("x", 1, 5, 5, 1025, 1025), protein, ff, 4).poses[0]
+    e32, e64 = oracle_batch(b)
+    ctx.upload_batch(b)
+    cfg, ms = ctx.autotune_batch(max_ms=500)
+    assert ms > 0
+    ctx.run_batch(cfg)
+    assert_parity(ctx.download_batch(), e32, e64)
+
+
+def test_batch_errors(ctx):
+    b = small_batch(n=3)
+    b.ligands[1] = b.ligands[1].copy()
+    b.ligands[1]["type"][0] = 99
+    with pytest.raises(BudeError) as ei:
+        ctx.upload_batch(b)
+    assert ei.value.code == BUDE_ERR_TYPE
+    with pytest.raises(BudeError) as ei:
+        ctx.run_batch(launch_cfg(8, 128))
+    assert ei.value.code == BUDE_ERR_STATE
+    ok = small_batch(n=3)
+    ctx.upload_batch(ok)
+    with pytest.raises(BudeError) as ei:
+        ctx.run_batch(launch_cfg(3, 128))
+    assert ei.value.code == BUDE_ERR_ARG
+    # uploading a deck replaces the batch
+    deck, _, _ = load_golden("small_head")
+    ctx.upload(deck)
+    with pytest.raises(BudeError):
+        ctx.run_batch(launch_cfg(8, 128))
