@@ -160,6 +160,80 @@ int bude_gpu_run_batch(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, int32_t pe
 /* Energies of the last batch evaluation, in concatenated pose order. */
 int bude_gpu_download_batch(bude_gpu_ctx *ctx, float *energies, int64_t total_poses);
 
+/* ---- Learned pre-screen (no counterpart in the reference) --------------------------------
+ * A per-protein MLP estimates pose energies: per (pose, ligand atom) features -- a 16-wide
+ * learned type embedding, the transformed atom position and 13 protein-field channels sampled
+ * from a grid precomputed for the protein -- go through 32 -> 128 -> 128 -> 128 -> 1 with SiLU;
+ * the outputs are summed per pose.  BF16 weights on BF16 tensor-core GEMMs with FP32
+ * accumulation; FP32 master weights and Adam state. */
+#define BUDE_SURROGATE_NPARAMS 38404
+
+/* Create (or reset) the context's surrogate for a protein: builds the field grid over
+ * [-extent, extent]^3 with `spacing` (at most 400 points a side) and seeds the weights.  At most
+ * 64 forcefield types. */
+int bude_surrogate_init(bude_gpu_ctx *ctx, const bude_atom *protein, int32_t natpro, const bude_ffparams *forcefield,
+                        int32_t ntypes, float extent, float spacing, uint64_t seed);
+
+/* Train on every pose of the uploaded batch (bude_gpu_upload_batch) for `epochs` epochs of
+ * shuffled batches of `batch_poses` poses with Adam (learning rate `lr`, cosine decay to lr/20).
+ * labels (NULL: exact energies computed here with the batched exact kernel) are per pose in batch
+ * order.  The loss is the mean squared error on the compressed scale 20*asinh(E/20).  final_loss
+ * (optional): mean loss of the last epoch; train_ms (optional): GPU time. */
+int bude_surrogate_train(bude_gpu_ctx *ctx, int32_t epochs, int32_t batch_poses, float lr, const float *labels,
+                         uint64_t seed, float *final_loss, float *train_ms);
+
+/* Surrogate energies of every pose of the uploaded batch (kept on the device; see
+ * bude_surrogate_download).  *ms (optional): CUDA-event time including the pose transforms. */
+int bude_surrogate_score(bude_gpu_ctx *ctx, float *ms);
+int bude_surrogate_download(bude_gpu_ctx *ctx, float *scores, int64_t n);
+
+/* Loss gradient (no update) over the given batch poses with the given per-pose labels:
+ * grads[BUDE_SURROGATE_NPARAMS] in the parameter layout, pred[n] the predicted energies. */
+int bude_surrogate_gradient(bude_gpu_ctx *ctx, const int32_t *poses, int32_t n, const float *labels, float *grads,
+                            float *pred);
+
+/* Features of the (pose, ligand atom) rows of the given batch poses, rows laid out pose by pose:
+ * features[rows][32] as the BF16 values the MLP sees (widened to float), types[rows] (optional)
+ * the atoms' forcefield types. */
+int bude_surrogate_features(bude_gpu_ctx *ctx, const int32_t *poses, int32_t n, float *features, int32_t *types);
+
+/* Read (out != NULL) and/or replace (in != NULL) the FP32 parameters, n = BUDE_SURROGATE_NPARAMS.
+ * Layout: embedding [64][16], W1 [128][32], b1, W2 [128][128], b2, W3 [128][128], b3, w4 [128],
+ * b4 (+3 unused). */
+int bude_surrogate_params(bude_gpu_ctx *ctx, float *out, const float *in, int64_t n);
+
+/* Checkpoint of the weights and the Adam state (flat binary file). */
+int bude_surrogate_save(bude_gpu_ctx *ctx, const char *path);
+int bude_surrogate_load(bude_gpu_ctx *ctx, const char *path);
+
+/* ---- Surrogate-screened scoring of the uploaded batch (no counterpart in the reference) ---- */
+typedef struct bude_screen_cfg {
+  float top_frac;     /* fraction of each ligand's poses rescored by the exact kernel (best surrogate) */
+  float audit_frac;   /* fraction of each ligand's poses rescored at random (audit sample) */
+  float audit_tol;    /* audit error above which a ligand is rescored exhaustively */
+  uint32_t seed;      /* audit sample */
+  bude_launch_cfg exact; /* launch shape of the exact rescoring (split/cluster unused) */
+} bude_screen_cfg;
+
+typedef struct bude_screen_stats {
+  float total_ms, surrogate_ms, rescore_ms, fallback_ms;
+  int64_t rescored_poses;  /* picks + audit */
+  int32_t fallback_ligands;
+  int64_t fallback_poses;
+  float max_audit_error;
+} bude_screen_stats;
+
+/* Surrogate scores every pose; per ligand the exact kernel rescores the top_frac best-scored poses
+ * and an audit sample; a ligand whose audit error -- RMS(surrogate - exact) over its audit poses
+ * / max(RMS deviation of those exact energies, 1) -- exceeds audit_tol is rescored exhaustively.
+ * Needs a trained (or loaded) surrogate and an uploaded batch. */
+int bude_screen_run(bude_gpu_ctx *ctx, const bude_screen_cfg *cfg, bude_screen_stats *stats);
+
+/* Final energies (exact where rescored, surrogate elsewhere), rescored flags (per pose) and the
+ * per-ligand audit errors of the last screen; any output may be NULL. */
+int bude_screen_download(bude_gpu_ctx *ctx, float *final_energies, uint8_t *rescored, float *audit_error,
+                         int64_t total_poses);
+
 /* Number of kernels this library launched on the context since it was created (the transform
  * and exact kernels count one each). */
 int bude_gpu_launch_count(const bude_gpu_ctx *ctx, int64_t *count);

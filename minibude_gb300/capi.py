@@ -42,6 +42,23 @@ class BudeLaunchCfg(ctypes.Structure):
         return "BudeLaunchCfg(%s)" % ", ".join(f"{k}={v}" for k, v in self.as_dict().items())
 
 
+class BudeScreenCfg(ctypes.Structure):
+    _fields_ = [("top_frac", ctypes.c_float), ("audit_frac", ctypes.c_float), ("audit_tol", ctypes.c_float),
+                ("seed", ctypes.c_uint32), ("exact", BudeLaunchCfg)]
+
+
+class BudeScreenStats(ctypes.Structure):
+    _fields_ = [("total_ms", ctypes.c_float), ("surrogate_ms", ctypes.c_float), ("rescore_ms", ctypes.c_float),
+                ("fallback_ms", ctypes.c_float), ("rescored_poses", c_int64), ("fallback_ligands", c_int32),
+                ("fallback_poses", c_int64), ("max_audit_error", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+SURROGATE_NPARAMS = 38404
+
+
 class BudeError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")
@@ -76,6 +93,19 @@ SIGNATURES = [
     ("bude_gpu_autotune_batch", ctypes.c_int, [_P, c_int32, ctypes.POINTER(BudeLaunchCfg), c_float_p]),
     ("bude_gpu_run_batch", ctypes.c_int, [_P, ctypes.POINTER(BudeLaunchCfg), c_int32, c_float_p]),
     ("bude_gpu_download_batch", ctypes.c_int, [_P, c_float_p, c_int64]),
+    ("bude_surrogate_init", ctypes.c_int, [_P, _P, c_int32, _P, c_int32, ctypes.c_float, ctypes.c_float,
+                                           ctypes.c_uint64]),
+    ("bude_surrogate_train", ctypes.c_int, [_P, c_int32, c_int32, ctypes.c_float, _P, ctypes.c_uint64, c_float_p,
+                                            c_float_p]),
+    ("bude_surrogate_score", ctypes.c_int, [_P, c_float_p]),
+    ("bude_surrogate_download", ctypes.c_int, [_P, c_float_p, c_int64]),
+    ("bude_surrogate_gradient", ctypes.c_int, [_P, _P, c_int32, _P, c_float_p, c_float_p]),
+    ("bude_surrogate_features", ctypes.c_int, [_P, _P, c_int32, c_float_p, _P]),
+    ("bude_surrogate_params", ctypes.c_int, [_P, c_float_p, c_float_p, c_int64]),
+    ("bude_surrogate_save", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("bude_surrogate_load", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("bude_screen_run", ctypes.c_int, [_P, ctypes.POINTER(BudeScreenCfg), ctypes.POINTER(BudeScreenStats)]),
+    ("bude_screen_download", ctypes.c_int, [_P, c_float_p, _P, c_float_p, c_int64]),
     ("bude_gpu_launch_count", ctypes.c_int, [_P, ctypes.POINTER(c_int64)]),
     ("bude_gpu_fasten_noalloc", ctypes.c_int, [_P, c_int32, _P, c_int32, _P, c_int32, _P, c_int64, c_int64, _P, _P]),
     ("bude_host_alloc", ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),

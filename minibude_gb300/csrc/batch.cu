@@ -166,22 +166,17 @@ static int batch_blocks_per_sm(const bude_launch_cfg &cfg, int *per_sm) {
   return rc;
 }
 
-// Enqueue one persistent evaluation (counter reset, transforms, batch kernel) for items already
-// on the device.
-static int enqueue_persistent(Context &c, const bude_launch_cfg &cfg, int grid, const int4 *items, int n_items) {
+// Enqueue the batch kernel over `items` (counter reset first): energies of the items' poses from
+// the transforms at `xform` into `energies`.
+static int enqueue_items(Context &c, const bude_launch_cfg &cfg, int grid, const int4 *items, int n_items,
+                         const float4 *xform, float *energies) {
   cudaError_t e = cudaMemsetAsync(c.b_counter.ptr, 0, sizeof(unsigned), c.stream);
   if (e != cudaSuccess) return cuda_error(e, "batch counter reset");
-  if (c.batch_poses > 0) {
-    const int tb = 256;
-    pose_xform_kernel<<<(unsigned)((c.batch_poses + tb - 1) / tb), tb, 0, c.stream>>>(
-        c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>());
-    c.launches++;
-  }
   BatchArgs a;
   a.ligands = c.b_ligands.as<float4>();
   a.slab = c.slab.as<float4>();
-  a.xform = c.b_xform.as<float>();
-  a.energies = c.b_energies.as<float>();
+  a.xform = reinterpret_cast<const float *>(xform);
+  a.energies = energies;
   a.items = items;
   a.counter = c.b_counter.as<unsigned>();
   a.err = c.err.as<unsigned>();
@@ -195,6 +190,18 @@ static int enqueue_persistent(Context &c, const bude_launch_cfg &cfg, int grid, 
   if (e != cudaSuccess) return cuda_error(e, "batch_kernel launch");
   c.launches++;
   return BUDE_OK;
+}
+
+// Enqueue one persistent evaluation of the whole batch (transforms, then the batch kernel) for
+// items already on the device.
+static int enqueue_persistent(Context &c, const bude_launch_cfg &cfg, int grid, const int4 *items, int n_items) {
+  if (c.batch_poses > 0) {
+    const int tb = 256;
+    pose_xform_kernel<<<(unsigned)((c.batch_poses + tb - 1) / tb), tb, 0, c.stream>>>(
+        c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>());
+    c.launches++;
+  }
+  return enqueue_items(c, cfg, grid, items, n_items, c.b_xform.as<float4>(), c.b_energies.as<float>());
 }
 
 static int persistent_grid(Context &c, const bude_launch_cfg &cfg, int *grid) {
@@ -235,6 +242,14 @@ static int ensure_graph(Context &c, const bude_launch_cfg &cfg) {
   }
   c.graph_cfg = cfg;
   return BUDE_OK;
+}
+
+int batch_items_enqueue(Context &c, const bude_launch_cfg &cfg, const int4 *items, int n_items, const float4 *xform,
+                        float *energies) {
+  int grid = 0;
+  int rc = persistent_grid(c, cfg, &grid);
+  if (rc) return rc;
+  return enqueue_items(c, cfg, grid, items, n_items, xform, energies);
 }
 
 int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand) {

@@ -373,6 +373,8 @@ void destroy_context(Context *c) {
   c->flush.release();
   c->partial.release();
   release_batch(*c);
+  release_surrogate(*c);
+  release_screen(*c);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);

@@ -10,6 +10,9 @@
 namespace bude {
 
 
+struct Surrogate;
+struct ScreenState;
+
 // A growable device allocation.
 struct DevBuf {
   void *ptr = nullptr;
@@ -46,6 +49,8 @@ struct Context {
   long long batch_tuned_key = -1;
   bude_launch_cfg batch_tuned{};
   float batch_tuned_ms = 0.f;
+  Surrogate *surrogate = nullptr; // learned pre-screen (surrogate.cu)
+  ScreenState *screen = nullptr;  // last screening run (screen.cu)
   // autotuner cache: the deck shape it was tuned for and the pick
   long long tuned_key[3] = {-1, -1, -1};
   bude_launch_cfg tuned{};
@@ -70,6 +75,13 @@ int exact_blocks_per_sm(const bude_launch_cfg &cfg, int *out);
 int choose_split(const Context &c, bude_launch_cfg &cfg);
 int choose_split_for(int num_sms, int natpro_pad, long long nposes, bude_launch_cfg &cfg);
 void release_batch(Context &c);
+int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand);
+int batch_items_enqueue(Context &c, const bude_launch_cfg &cfg, const int4 *items, int n_items, const float4 *xform,
+                        float *energies);
+void release_surrogate(Context &c);
+void release_screen(Context &c);
+int surrogate_score_enqueue(Context &c, const float4 *xform_ready);
+float *surrogate_scores(Context &c);
 int autotune(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms);
 int default_cfg(const Context &c, int ppwi, int wgsize, bude_launch_cfg &cfg);
 int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid = nullptr);

@@ -1,0 +1,720 @@
+// surrogate.cu -- host side of the learned pre-screen (kernels in surrogate_kernels.cuh).
+//
+// No counterpart in the reference.  A per-protein MLP is trained on exact energies of the
+// context's uploaded batch (computed here with the batched exact kernel) and then scores poses
+// for the screening pipeline (screen.cu), where the exact kernel rescores its picks and remains
+// the judge.  Forward, backward and Adam are hand-written kernels driven from this file; every
+// reduction (weight, bias and embedding gradients, the loss) is summed in a fixed order, so a
+// training run is deterministic for a given seed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <vector>
+
+#include "exact_kernel.cuh"
+#include "internal.h"
+#include "surrogate_kernels.cuh"
+
+namespace bude {
+
+// FP32 parameter layout (masters, Adam moments and gradients share it).
+constexpr long long kOffEmb = 0;
+constexpr long long kOffW1 = kOffEmb + kMaxTypes * kEmb;
+constexpr long long kOffB1 = kOffW1 + kHid * kFeat;
+constexpr long long kOffW2 = kOffB1 + kHid;
+constexpr long long kOffB2 = kOffW2 + kHid * kHid;
+constexpr long long kOffW3 = kOffB2 + kHid;
+constexpr long long kOffB3 = kOffW3 + kHid * kHid;
+constexpr long long kOffW4 = kOffB3 + kHid;
+constexpr long long kOffB4 = kOffW4 + kHid;
+constexpr long long kNParams = kOffB4 + 4;
+
+static_assert(kNParams == BUDE_SURROGATE_NPARAMS, "parameter count in the header must match");
+
+struct Surrogate {
+  bool ready = false;
+  int ntypes = 0;
+  DevBuf params, adam_m, adam_v, grads;
+  DevBuf emb_bf, w1_bf, w2_bf, w3_bf, w1t_bf, w2t_bf, w3t_bf;
+  DevBuf grid, protein4;
+  FieldGrid fg{};
+  long long step = 0;
+  // training scratch
+  DevBuf X, row_type, Z1, Z2, Z3, dZ1, dZ2, dZ3, y, dy, pred, loss, part_w4, part_b, part_emb, part_w;
+  DevBuf labels, pose_lig_first, pose_lig_n, epoch_pose, epoch_rowoff;
+  long long rows_cap = 0;
+  // scoring
+  DevBuf items, scores;
+  int items_for = 0;
+  int n_items = 0;
+};
+
+static Surrogate &sur(Context &c) {
+  if (!c.surrogate) c.surrogate = new Surrogate();
+  return *c.surrogate;
+}
+
+void release_surrogate(Context &c) {
+  if (!c.surrogate) return;
+  Surrogate &s = *c.surrogate;
+  DevBuf *all[] = {&s.params, &s.adam_m, &s.adam_v, &s.grads, &s.emb_bf, &s.w1_bf, &s.w2_bf, &s.w3_bf,
+                   &s.w1t_bf, &s.w2t_bf, &s.w3t_bf, &s.grid, &s.protein4, &s.X, &s.row_type, &s.Z1,
+                   &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3, &s.y, &s.dy, &s.pred, &s.loss, &s.part_w4,
+                   &s.part_b, &s.part_emb, &s.part_w, &s.labels, &s.pose_lig_first, &s.pose_lig_n,
+                   &s.epoch_pose, &s.epoch_rowoff, &s.items, &s.scores};
+  for (DevBuf *b : all) b->release();
+  delete c.surrogate;
+  c.surrogate = nullptr;
+}
+
+static MlpWeights weights(Surrogate &s) {
+  MlpWeights W;
+  W.emb = s.emb_bf.as<__nv_bfloat16>();
+  W.w1 = s.w1_bf.as<__nv_bfloat16>();
+  W.w2 = s.w2_bf.as<__nv_bfloat16>();
+  W.w3 = s.w3_bf.as<__nv_bfloat16>();
+  const float *p = s.params.as<float>();
+  W.b1 = p + kOffB1;
+  W.b2 = p + kOffB2;
+  W.b3 = p + kOffB3;
+  W.w4 = p + kOffW4;
+  W.b4 = p + kOffB4;
+  return W;
+}
+
+// Refresh the BF16 copies of the weights from the FP32 masters.
+static int publish(Context &c, Surrogate &s) {
+  const float *p = s.params.as<float>();
+  auto launch = [&](long long off, int rows, int cols, DevBuf *plain, DevBuf *trans) {
+    const int n = rows * cols;
+    publish_kernel<<<(n + 255) / 256, 256, 0, c.stream>>>(p + off, rows, cols,
+                                                          plain ? plain->as<__nv_bfloat16>() : nullptr,
+                                                          trans ? trans->as<__nv_bfloat16>() : nullptr);
+  };
+  launch(kOffEmb, kMaxTypes, kEmb, &s.emb_bf, nullptr);
+  launch(kOffW1, kHid, kFeat, &s.w1_bf, &s.w1t_bf);
+  launch(kOffW2, kHid, kHid, &s.w2_bf, &s.w2t_bf);
+  launch(kOffW3, kHid, kHid, &s.w3_bf, &s.w3t_bf);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "surrogate publish");
+}
+
+static int set_smem_limits() {
+  static bool done = false;
+  if (done) return BUDE_OK;
+  cudaError_t e = cudaFuncSetAttribute(score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(train_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(train_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(BwdSmem));
+  if (e != cudaSuccess) return cuda_error(e, "surrogate shared-memory limits");
+  done = true;
+  return BUDE_OK;
+}
+
+// The protein of the context (kept from the last upload) as float4 records for the grid kernel.
+int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes, float extent,
+                   float spacing, unsigned long long seed) {
+  if (ntypes <= 0 || ntypes > kMaxTypes)
+    return set_error(BUDE_ERR_ARG, "the surrogate supports 1..%d forcefield types (got %d)", kMaxTypes, ntypes);
+  if (!(extent > 0.f) || !(spacing > 0.f) || extent / spacing > 200.f)
+    return set_error(BUDE_ERR_ARG, "bad grid extent %g / spacing %g (at most 400 points a side)", extent, spacing);
+  if (natpro < 0 || (natpro > 0 && !protein) || !ff) return set_error(BUDE_ERR_ARG, "bad protein");
+  for (int i = 0; i < natpro; ++i)
+    if (protein[i].type < 0 || protein[i].type >= ntypes)
+      return set_error(BUDE_ERR_TYPE, "protein atom %d has type %d outside the forcefield", i, protein[i].type);
+  int rc = set_smem_limits();
+  if (rc) return rc;
+  Surrogate &s = sur(c);
+  s.ready = false;
+  s.ntypes = ntypes;
+  s.step = 0;
+  // Parameters: torch-Linear-style uniform(+-1/sqrt(fan_in)) weights and biases, N(0,1) embedding.
+  std::vector<float> p(kNParams, 0.f);
+  std::mt19937_64 rng(seed);
+  std::normal_distribution<float> nd(0.f, 1.f);
+  for (long long i = 0; i < kMaxTypes * kEmb; ++i) p[kOffEmb + i] = nd(rng);
+  auto uni = [&](long long off, long long n, int fan_in) {
+    std::uniform_real_distribution<float> ud(-1.f / std::sqrt((float)fan_in), 1.f / std::sqrt((float)fan_in));
+    for (long long i = 0; i < n; ++i) p[off + i] = ud(rng);
+  };
+  uni(kOffW1, kHid * kFeat, kFeat);
+  uni(kOffB1, kHid, kFeat);
+  uni(kOffW2, kHid * kHid, kHid);
+  uni(kOffB2, kHid, kHid);
+  uni(kOffW3, kHid * kHid, kHid);
+  uni(kOffB3, kHid, kHid);
+  uni(kOffW4, kHid, kHid);
+  uni(kOffB4, 1, kHid);
+  const size_t pb = kNParams * sizeof(float);
+  rc = s.params.reserve(pb, "surrogate params");
+  if (!rc) rc = s.adam_m.reserve(pb, "adam m");
+  if (!rc) rc = s.adam_v.reserve(pb, "adam v");
+  if (!rc) rc = s.grads.reserve(pb, "surrogate grads");
+  if (!rc) rc = s.emb_bf.reserve(kMaxTypes * kEmb * 2, "emb bf16");
+  if (!rc) rc = s.w1_bf.reserve(kHid * kFeat * 2, "w1 bf16");
+  if (!rc) rc = s.w1t_bf.reserve(kHid * kFeat * 2, "w1t bf16");
+  if (!rc) rc = s.w2_bf.reserve(kHid * kHid * 2, "w2 bf16");
+  if (!rc) rc = s.w2t_bf.reserve(kHid * kHid * 2, "w2t bf16");
+  if (!rc) rc = s.w3_bf.reserve(kHid * kHid * 2, "w3 bf16");
+  if (!rc) rc = s.w3t_bf.reserve(kHid * kHid * 2, "w3t bf16");
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(s.params.ptr, p.data(), pb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(s.adam_m.ptr, 0, pb);
+  if (e == cudaSuccess) e = cudaMemset(s.adam_v.ptr, 0, pb);
+  if (e != cudaSuccess) return cuda_error(e, "surrogate init");
+
+  // Field grid over [-extent, extent]^3.
+  const int n = (int)std::ceil(2.f * extent / spacing) + 1;
+  const long long nvox = (long long)n * n * n;
+  rc = s.grid.reserve((size_t)nvox * 16 * sizeof(float), "field grid");
+  if (!rc) rc = s.protein4.reserve((size_t)std::max(natpro, 1) * 16, "grid protein");
+  DevBuf dff, inv;
+  if (!rc) rc = dff.reserve((size_t)ntypes * sizeof(bude_ffparams), "grid forcefield");
+  if (!rc) rc = inv.reserve(16 * sizeof(float), "grid scales");
+  if (rc) return rc;
+  if (natpro > 0) cudaMemcpy(s.protein4.ptr, protein, (size_t)natpro * 16, cudaMemcpyHostToDevice);
+  cudaMemcpy(dff.ptr, ff, (size_t)ntypes * sizeof(bude_ffparams), cudaMemcpyHostToDevice);
+  GridBuild gb;
+  gb.protein = s.protein4.as<float4>();
+  gb.ff = dff.as<bude_ffparams>();
+  gb.natpro = natpro;
+  gb.ox = gb.oy = gb.oz = -extent;
+  gb.h = spacing;
+  gb.nx = gb.ny = gb.nz = n;
+  gb.out = s.grid.as<float>();
+  grid_kernel<<<(unsigned)((nvox + 127) / 128), 128, 0, c.stream>>>(gb);
+  e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) {
+    dff.release();
+    inv.release();
+    return cuda_error(e, "field grid");
+  }
+  // Unit standard deviation per channel (a zero channel keeps scale 1).
+  std::vector<float> h((size_t)nvox * 16);
+  cudaMemcpy(h.data(), s.grid.ptr, h.size() * sizeof(float), cudaMemcpyDeviceToHost);
+  float scale[16];
+  for (int k = 0; k < 16; ++k) {
+    double m = 0, m2 = 0;
+    for (long long v = 0; v < nvox; ++v) {
+      const double x = h[(size_t)v * 16 + k];
+      m += x;
+      m2 += x * x;
+    }
+    m /= (double)nvox;
+    const double var = std::max(0.0, m2 / (double)nvox - m * m);
+    scale[k] = var > 1e-12 ? (float)(1.0 / std::sqrt(var)) : 1.f;
+  }
+  cudaMemcpy(inv.ptr, scale, sizeof scale, cudaMemcpyHostToDevice);
+  grid_scale_kernel<<<(unsigned)((nvox * 16 + 255) / 256), 256, 0, c.stream>>>(s.grid.as<float>(), nvox,
+                                                                             inv.as<float>());
+  e = cudaStreamSynchronize(c.stream);
+  dff.release();
+  inv.release();
+  if (e != cudaSuccess) return cuda_error(e, "field grid scaling");
+  s.fg.data = s.grid.as<float4>();
+  s.fg.ox = s.fg.oy = s.fg.oz = -extent;
+  s.fg.inv_h = 1.f / spacing;
+  s.fg.nx = s.fg.ny = s.fg.nz = n;
+  s.fg.xyz_scale = 0.1f;
+  rc = publish(c, s);
+  if (rc) return rc;
+  s.ready = true;
+  return BUDE_OK;
+}
+
+static int ensure_train_scratch(Surrogate &s, long long rows, int batch, int nblk, int nchunks) {
+  int rc = BUDE_OK;
+  if (rows > s.rows_cap) {
+    const size_t r = (size_t)rows;
+    rc = s.X.reserve(r * kFeat * 2, "X");
+    if (!rc) rc = s.row_type.reserve(r * 4, "row types");
+    for (DevBuf *b : {&s.Z1, &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3})
+      if (!rc) rc = b->reserve(r * kHid * 2, "activations");
+    if (!rc) rc = s.y.reserve(r * 4, "y");
+    if (!rc) rc = s.dy.reserve(r * 4, "dy");
+    if (rc) return rc;
+    s.rows_cap = rows;
+  }
+  if (!rc) rc = s.pred.reserve((size_t)batch * 4, "pred");
+  if (!rc) rc = s.loss.reserve((size_t)batch * 4, "loss");
+  if (!rc) rc = s.part_w4.reserve((size_t)nblk * kHid * 4, "w4 parts");
+  if (!rc) rc = s.part_b.reserve((size_t)nblk * 4 * kHid * 4, "bias parts");
+  if (!rc) rc = s.part_emb.reserve((size_t)nblk * kMaxTypes * kEmb * 4, "embedding parts");
+  if (!rc) rc = s.part_w.reserve((size_t)nchunks * kHid * kHid * 4, "weight parts");
+  return rc;
+}
+
+// One optimisation step on `nb` poses whose indices/row offsets are at dpose/drowoff.
+static int train_step(Context &c, Surrogate &s, const int *dpose, const int *drowoff, int nb, long long rows, float lr,
+                      float *loss_sum_dev_host) {
+  const float *p = s.params.as<float>();
+  float *gr = s.grads.as<float>();
+  RowMap m;
+  m.pose = dpose;
+  m.row_off = drowoff;
+  m.lig_first = s.pose_lig_first.as<int>();
+  m.lig_n = s.pose_lig_n.as<int>();
+  m.nposes = nb;
+  const MlpWeights W = weights(s);
+  const int tiles = (int)((rows + kRowsPerCta - 1) / kRowsPerCta);
+  const int nblk = std::min(tiles, 2 * std::max(c.num_sms, 1));
+  const int chunk = 2048;
+  const int nchunks = (int)((rows + chunk - 1) / chunk);
+  int rc = ensure_train_scratch(s, rows, nb, nblk, nchunks);
+  if (rc) return rc;
+  train_features_kernel<<<(nb * 32 + 255) / 256, 256, 0, c.stream>>>(W, s.fg, c.b_ligands.as<float4>(),
+                                                                       c.b_xform.as<float4>(), m,
+                                                                       s.X.as<__nv_bfloat16>(), s.row_type.as<int>());
+  train_forward_kernel<<<nblk, kMlpThreads, sizeof(MlpSmem), c.stream>>>(
+      W, s.X.as<__nv_bfloat16>(), (int)rows, s.Z1.as<__nv_bfloat16>(), s.Z2.as<__nv_bfloat16>(),
+      s.Z3.as<__nv_bfloat16>(), s.y.as<float>());
+  train_loss_kernel<<<(nb + 127) / 128, 128, 0, c.stream>>>(m, s.y.as<float>(), p + kOffB4, s.labels.as<float>(),
+                                                          s.pred.as<float>(), s.loss.as<float>(), s.dy.as<float>(),
+                                                          1.f / (float)nb);
+  BwdArgs b;
+  b.w1t = s.w1t_bf.as<__nv_bfloat16>();
+  b.w2t = s.w2t_bf.as<__nv_bfloat16>();
+  b.w3t = s.w3t_bf.as<__nv_bfloat16>();
+  b.w4 = p + kOffW4;
+  b.Z1 = s.Z1.as<__nv_bfloat16>();
+  b.Z2 = s.Z2.as<__nv_bfloat16>();
+  b.Z3 = s.Z3.as<__nv_bfloat16>();
+  b.dy = s.dy.as<float>();
+  b.row_type = s.row_type.as<int>();
+  b.rows = (int)rows;
+  b.dZ1 = s.dZ1.as<__nv_bfloat16>();
+  b.dZ2 = s.dZ2.as<__nv_bfloat16>();
+  b.dZ3 = s.dZ3.as<__nv_bfloat16>();
+  b.part_w4 = s.part_w4.as<float>();
+  b.part_b = s.part_b.as<float>();
+  b.part_emb = s.part_emb.as<float>();
+  train_backward_kernel<<<nblk, kMlpThreads, sizeof(BwdSmem), c.stream>>>(b);
+  auto reduce = [&](const float *part, int nparts, long long n, long long stride, float *dst) {
+    reduce_parts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c.stream>>>(part, nparts, n, stride, dst);
+  };
+  // layer weight gradients
+  struct L { const __nv_bfloat16 *dz, *hin; int kin, silu; long long off; };
+  const L layers[3] = {{s.dZ3.as<__nv_bfloat16>(), s.Z2.as<__nv_bfloat16>(), kHid, 1, kOffW3},
+                       {s.dZ2.as<__nv_bfloat16>(), s.Z1.as<__nv_bfloat16>(), kHid, 1, kOffW2},
+                       {s.dZ1.as<__nv_bfloat16>(), s.X.as<__nv_bfloat16>(), kFeat, 0, kOffW1}};
+  for (const L &l : layers) {
+    WgradArgs w;
+    w.dZ = l.dz;
+    w.Hin = l.hin;
+    w.apply_silu = l.silu;
+    w.rows = (int)rows;
+    w.chunk_rows = chunk;
+    w.part = s.part_w.as<float>();
+    if (l.kin == kHid) wgrad_kernel<kHid><<<nchunks, kMlpThreads, 0, c.stream>>>(w);
+    else wgrad_kernel<kFeat><<<nchunks, kMlpThreads, 0, c.stream>>>(w);
+    reduce(s.part_w.as<float>(), nchunks, (long long)kHid * l.kin, (long long)kHid * l.kin, gr + l.off);
+  }
+  reduce(s.part_w4.as<float>(), nblk, kHid, kHid, gr + kOffW4);
+  reduce(s.part_b.as<float>(), nblk, kHid, 4 * kHid, gr + kOffB1);
+  reduce(s.part_b.as<float>() + kHid, nblk, kHid, 4 * kHid, gr + kOffB2);
+  reduce(s.part_b.as<float>() + 2 * kHid, nblk, kHid, 4 * kHid, gr + kOffB3);
+  reduce(s.part_b.as<float>() + 3 * kHid, nblk, 1, 4 * kHid, gr + kOffB4);
+  reduce(s.part_emb.as<float>(), nblk, kMaxTypes * kEmb, kMaxTypes * kEmb, gr + kOffEmb);
+  if (lr > 0.f) {
+    s.step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float lr_t = lr * std::sqrt(1.f - std::pow(b2, (float)s.step)) / (1.f - std::pow(b1, (float)s.step));
+    adam_kernel<<<(unsigned)((kNParams + 255) / 256), 256, 0, c.stream>>>(
+        s.params.as<float>(), s.adam_m.as<float>(), s.adam_v.as<float>(), gr, kNParams, lr_t, b1, b2, 1e-8f);
+    rc = publish(c, s);
+    if (rc) return rc;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "surrogate training step");
+  (void)loss_sum_dev_host;
+  return BUDE_OK;
+}
+
+// Pose -> (first ligand atom, natlig) for every pose of the uploaded batch.
+static int upload_pose_ligands(Context &c, Surrogate &s, std::vector<int> &lig_n) {
+  const long long np = c.batch_poses;
+  std::vector<int> first((size_t)np);
+  lig_n.assign((size_t)np, 0);
+  for (int l = 0; l < c.nligands; ++l)
+    for (long long p = c.pose_off[l]; p < c.pose_off[l + 1]; ++p) {
+      first[(size_t)p] = c.lig_off[l];
+      lig_n[(size_t)p] = c.lig_off[l + 1] - c.lig_off[l];
+    }
+  int rc = s.pose_lig_first.reserve((size_t)std::max(np, 1LL) * 4, "pose ligands");
+  if (!rc) rc = s.pose_lig_n.reserve((size_t)std::max(np, 1LL) * 4, "pose ligands");
+  if (rc) return rc;
+  if (np > 0) {
+    cudaMemcpy(s.pose_lig_first.ptr, first.data(), (size_t)np * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(s.pose_lig_n.ptr, lig_n.data(), (size_t)np * 4, cudaMemcpyHostToDevice);
+  }
+  return BUDE_OK;
+}
+
+static int batch_transforms(Context &c) {
+  if (c.batch_poses == 0) return BUDE_OK;
+  const int tb = 256;
+  pose_xform_kernel<<<(unsigned)((c.batch_poses + tb - 1) / tb), tb, 0, c.stream>>>(
+      c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>());
+  c.launches++;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "pose transforms");
+}
+
+// The batch's atom types index the surrogate's embedding table.
+static int check_batch_types(const Context &c) {
+  if (c.ntypes > kMaxTypes)
+    return set_error(BUDE_ERR_ARG, "the uploaded batch has %d forcefield types; the surrogate embeds at most %d",
+                     c.ntypes, kMaxTypes);
+  return BUDE_OK;
+}
+
+int surrogate_train(Context &c, int epochs, int batch, float lr, const float *labels, float *final_loss,
+                    float *train_ms, unsigned long long seed) {
+  Surrogate &s = sur(c);
+  if (!s.ready) return set_error(BUDE_ERR_STATE, "surrogate not initialised");
+  if (!c.have_batch) return set_error(BUDE_ERR_STATE, "no batch uploaded");
+  if (check_batch_types(c)) return BUDE_ERR_ARG;
+  if (epochs < 0 || batch <= 0) return set_error(BUDE_ERR_ARG, "bad epochs/batch");
+  const long long np = c.batch_poses;
+  if (np == 0) return set_error(BUDE_ERR_ARG, "empty batch");
+  int rc = s.labels.reserve((size_t)np * 4, "labels");
+  if (rc) return rc;
+  if (labels) {
+    cudaMemcpy(s.labels.ptr, labels, (size_t)np * 4, cudaMemcpyHostToDevice);
+  } else {
+    // Labels: exact energies of every pose from the batched exact kernel.
+    bude_launch_cfg cfg{16, 128, 1, 64, 1, 0};
+    rc = enqueue_batch(c, cfg, 0);
+    if (!rc) rc = check_device_error(c);
+    if (rc) return rc;
+    cudaMemcpyAsync(s.labels.ptr, c.b_energies.ptr, (size_t)np * 4, cudaMemcpyDeviceToDevice, c.stream);
+  }
+  std::vector<int> lig_n;
+  rc = upload_pose_ligands(c, s, lig_n);
+  if (!rc) rc = batch_transforms(c);
+  if (rc) return rc;
+  // b4 starts at the mean label per ligand atom.
+  if (s.step == 0) {
+    std::vector<float> hl((size_t)np);
+    cudaMemcpy(hl.data(), s.labels.ptr, (size_t)np * 4, cudaMemcpyDeviceToHost);
+    double sl = 0, sa = 0;
+    for (long long p = 0; p < np; ++p) {
+      sl += std::asinh(hl[(size_t)p] / kLossScale) * kLossScale;
+      sa += lig_n[(size_t)p];
+    }
+    const float b4 = (float)(sl / std::max(sa, 1.0));
+    cudaMemcpy(s.params.as<float>() + kOffB4, &b4, sizeof b4, cudaMemcpyHostToDevice);
+  }
+  const int nb_full = (int)std::min<long long>(batch, np);
+  const int steps_per_epoch = (int)((np + nb_full - 1) / nb_full);
+  const long long total_steps = (long long)epochs * steps_per_epoch;
+  std::vector<int> order((size_t)np), rowoff;
+  std::iota(order.begin(), order.end(), 0);
+  std::mt19937_64 rng(seed);
+  rc = s.epoch_pose.reserve((size_t)np * 4, "epoch poses");
+  if (!rc) rc = s.epoch_rowoff.reserve((size_t)(np + steps_per_epoch) * 4, "epoch row offsets");
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c.stream);
+  double last_loss = 0;
+  long long done = 0;
+  for (int ep = 0; ep < epochs && !rc; ++ep) {
+    std::shuffle(order.begin(), order.end(), rng);
+    // Row offsets of every batch of the epoch, one block of (batch + 1) entries per step.
+    rowoff.clear();
+    std::vector<long long> rows_of(steps_per_epoch);
+    for (int st = 0; st < steps_per_epoch; ++st) {
+      const long long a = (long long)st * nb_full, b = std::min(np, a + nb_full);
+      int r = 0;
+      for (long long i = a; i < b; ++i) {
+        rowoff.push_back(r);
+        r += lig_n[(size_t)order[(size_t)i]];
+      }
+      rowoff.push_back(r);
+      rows_of[st] = r;
+    }
+    cudaMemcpyAsync(s.epoch_pose.ptr, order.data(), (size_t)np * 4, cudaMemcpyHostToDevice, c.stream);
+    cudaMemcpyAsync(s.epoch_rowoff.ptr, rowoff.data(), rowoff.size() * 4, cudaMemcpyHostToDevice, c.stream);
+    cudaStreamSynchronize(c.stream); // the host vectors are rewritten next epoch
+    double loss_sum = 0;
+    long long ro = 0;
+    for (int st = 0; st < steps_per_epoch && !rc; ++st) {
+      const long long a = (long long)st * nb_full, b = std::min(np, a + nb_full);
+      const int nb = (int)(b - a);
+      // Cosine decay from lr to lr / 20 over the run.
+      const double frac = total_steps > 1 ? (double)done / (double)(total_steps - 1) : 0.0;
+      const float lr_now = (float)(lr * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(M_PI * frac))));
+      rc = train_step(c, s, s.epoch_pose.as<int>() + a, s.epoch_rowoff.as<int>() + ro, nb, rows_of[st], lr_now,
+                      nullptr);
+      ro += nb + 1;
+      ++done;
+      if (!rc && ep == epochs - 1) {
+        std::vector<float> lh((size_t)nb);
+        cudaMemcpy(lh.data(), s.loss.ptr, (size_t)nb * 4, cudaMemcpyDeviceToHost);
+        for (float v : lh) loss_sum += v;
+      }
+    }
+    last_loss = loss_sum / (double)np;
+  }
+  cudaEventRecord(e1, c.stream);
+  cudaError_t e = cudaStreamSynchronize(c.stream);
+  if (!rc && e != cudaSuccess) rc = cuda_error(e, "surrogate training");
+  if (!rc && train_ms) cudaEventElapsedTime(train_ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!rc && final_loss) *final_loss = (float)last_loss;
+  return rc;
+}
+
+// One gradient of the loss over the given poses of the batch (no update); for tests.
+int surrogate_gradient(Context &c, const int *poses, int n, const float *labels, float *grad_out, float *pred_out) {
+  Surrogate &s = sur(c);
+  if (!s.ready || !c.have_batch) return set_error(BUDE_ERR_STATE, "surrogate or batch missing");
+  if (check_batch_types(c)) return BUDE_ERR_ARG;
+  const long long np = c.batch_poses;
+  std::vector<int> lig_n;
+  int rc = upload_pose_ligands(c, s, lig_n);
+  if (!rc) rc = batch_transforms(c);
+  if (!rc) rc = s.labels.reserve((size_t)np * 4, "labels");
+  if (!rc) rc = s.epoch_pose.reserve((size_t)n * 4, "poses");
+  if (!rc) rc = s.epoch_rowoff.reserve((size_t)(n + 1) * 4, "row offsets");
+  if (rc) return rc;
+  cudaMemcpy(s.labels.ptr, labels, (size_t)np * 4, cudaMemcpyHostToDevice);
+  std::vector<int> ro(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    if (poses[i] < 0 || poses[i] >= np) return set_error(BUDE_ERR_ARG, "pose index out of range");
+    ro[i + 1] = ro[i] + lig_n[(size_t)poses[i]];
+  }
+  cudaMemcpy(s.epoch_pose.ptr, poses, (size_t)n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s.epoch_rowoff.ptr, ro.data(), ro.size() * 4, cudaMemcpyHostToDevice);
+  rc = train_step(c, s, s.epoch_pose.as<int>(), s.epoch_rowoff.as<int>(), n, ro[n], 0.f, nullptr);
+  cudaError_t e = cudaStreamSynchronize(c.stream);
+  if (!rc && e != cudaSuccess) rc = cuda_error(e, "surrogate gradient");
+  if (rc) return rc;
+  if (grad_out) cudaMemcpy(grad_out, s.grads.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  if (pred_out) cudaMemcpy(pred_out, s.pred.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  return BUDE_OK;
+}
+
+// Features (as floats) and atom types of the rows of the given poses; for inspection and tests.
+int surrogate_features(Context &c, const int *poses, int n, float *X, int *types) {
+  Surrogate &s = sur(c);
+  if (!s.ready || !c.have_batch) return set_error(BUDE_ERR_STATE, "surrogate or batch missing");
+  if (check_batch_types(c)) return BUDE_ERR_ARG;
+  std::vector<int> lig_n;
+  int rc = upload_pose_ligands(c, s, lig_n);
+  if (!rc) rc = batch_transforms(c);
+  if (rc) return rc;
+  std::vector<int> ro(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    if (poses[i] < 0 || poses[i] >= c.batch_poses) return set_error(BUDE_ERR_ARG, "pose index out of range");
+    ro[i + 1] = ro[i] + lig_n[(size_t)poses[i]];
+  }
+  const long long rows = ro[n];
+  rc = s.epoch_pose.reserve((size_t)n * 4, "poses");
+  if (!rc) rc = s.epoch_rowoff.reserve((size_t)(n + 1) * 4, "row offsets");
+  if (!rc) rc = ensure_train_scratch(s, std::max(rows, 1LL), n, 1, 1);
+  if (rc) return rc;
+  cudaMemcpy(s.epoch_pose.ptr, poses, (size_t)n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s.epoch_rowoff.ptr, ro.data(), ro.size() * 4, cudaMemcpyHostToDevice);
+  RowMap m;
+  m.pose = s.epoch_pose.as<int>();
+  m.row_off = s.epoch_rowoff.as<int>();
+  m.lig_first = s.pose_lig_first.as<int>();
+  m.lig_n = s.pose_lig_n.as<int>();
+  m.nposes = n;
+  train_features_kernel<<<(n * 32 + 255) / 256, 256, 0, c.stream>>>(weights(s), s.fg, c.b_ligands.as<float4>(),
+                                                                      c.b_xform.as<float4>(), m,
+                                                                      s.X.as<__nv_bfloat16>(), s.row_type.as<int>());
+  cudaError_t e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) return cuda_error(e, "surrogate features");
+  std::vector<uint16_t> xb((size_t)rows * kFeat);
+  cudaMemcpy(xb.data(), s.X.ptr, xb.size() * 2, cudaMemcpyDeviceToHost);
+  for (size_t i = 0; i < xb.size(); ++i) {
+    const uint32_t u = (uint32_t)xb[i] << 16;
+    std::memcpy(&X[i], &u, 4);
+  }
+  if (types) cudaMemcpy(types, s.row_type.ptr, (size_t)rows * 4, cudaMemcpyDeviceToHost);
+  return BUDE_OK;
+}
+
+// Surrogate energies of every pose of the uploaded batch into s.scores (device).
+int surrogate_score_enqueue(Context &c, const float4 *xform_ready) {
+  Surrogate &s = sur(c);
+  if (!s.ready) return set_error(BUDE_ERR_STATE, "surrogate not initialised");
+  if (!c.have_batch) return set_error(BUDE_ERR_STATE, "no batch uploaded");
+  if (check_batch_types(c)) return BUDE_ERR_ARG;
+  const long long np = c.batch_poses;
+  int rc = s.scores.reserve((size_t)std::max(np, 1LL) * 4, "surrogate scores");
+  if (rc) return rc;
+  if (s.items_for != (int)np || s.n_items == 0) {
+    std::vector<int4> items;
+    for (int l = 0; l < c.nligands; ++l)
+      for (long long p = c.pose_off[l]; p < c.pose_off[l + 1]; p += kRowsPerCta)
+        items.push_back(make_int4(c.lig_off[l], c.lig_off[l + 1] - c.lig_off[l], (int)p,
+                                  (int)std::min<long long>(kRowsPerCta, c.pose_off[l + 1] - p)));
+    rc = s.items.reserve(std::max<size_t>(items.size(), 1) * sizeof(int4), "surrogate items");
+    if (rc) return rc;
+    if (!items.empty()) cudaMemcpy(s.items.ptr, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice);
+    s.n_items = (int)items.size();
+    s.items_for = (int)np;
+  }
+  if (!xform_ready) {
+    rc = batch_transforms(c);
+    if (rc) return rc;
+  }
+  if (s.n_items == 0) return BUDE_OK;
+  rc = set_smem_limits();
+  if (rc) return rc;
+  ScoreArgs a;
+  a.W = weights(s);
+  a.g = s.fg;
+  a.ligands = c.b_ligands.as<float4>();
+  a.xform = c.b_xform.as<float4>();
+  a.items = s.items.as<int4>();
+  a.scores = s.scores.as<float>();
+  a.n_items = s.n_items;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, score_kernel, kMlpThreads, sizeof(MlpSmem));
+  const int grid = std::min(s.n_items, std::max(1, per_sm) * std::max(c.num_sms, 1));
+  score_kernel<<<grid, kMlpThreads, sizeof(MlpSmem), c.stream>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "score_kernel launch");
+  c.launches++;
+  return BUDE_OK;
+}
+
+float *surrogate_scores(Context &c) { return c.surrogate ? c.surrogate->scores.as<float>() : nullptr; }
+
+int surrogate_io(Context &c, float *out, const float *in, long long n) {
+  Surrogate &s = sur(c);
+  if (!s.ready) return set_error(BUDE_ERR_STATE, "surrogate not initialised");
+  if (n != kNParams) return set_error(BUDE_ERR_ARG, "parameter vector has %lld values, not %lld", n, kNParams);
+  if (out) cudaMemcpy(out, s.params.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  if (in) {
+    cudaMemcpy(s.params.ptr, in, kNParams * 4, cudaMemcpyHostToDevice);
+    int rc = publish(c, s);
+    if (rc) return rc;
+  }
+  cudaError_t e = cudaStreamSynchronize(c.stream);
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "surrogate parameters");
+}
+
+// Checkpoint: magic, version, step, then masters, Adam m and Adam v (FP32).
+int surrogate_save(Context &c, const char *path) {
+  Surrogate &s = sur(c);
+  if (!s.ready) return set_error(BUDE_ERR_STATE, "surrogate not initialised");
+  std::vector<float> buf(3 * kNParams);
+  cudaMemcpy(buf.data(), s.params.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(buf.data() + kNParams, s.adam_m.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(buf.data() + 2 * kNParams, s.adam_v.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return set_error(BUDE_ERR_ARG, "cannot write %s", path);
+  const unsigned long long hdr[3] = {0x4255444553555231ull /* "BUDESUR1" */, (unsigned long long)kNParams,
+                                     (unsigned long long)s.step};
+  bool ok = std::fwrite(hdr, sizeof hdr, 1, f) == 1 && std::fwrite(buf.data(), 4, buf.size(), f) == buf.size();
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? BUDE_OK : set_error(BUDE_ERR_ARG, "short write to %s", path);
+}
+
+int surrogate_load(Context &c, const char *path) {
+  Surrogate &s = sur(c);
+  if (!s.ready) return set_error(BUDE_ERR_STATE, "initialise the surrogate (grid) before loading weights");
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return set_error(BUDE_ERR_ARG, "cannot read %s", path);
+  unsigned long long hdr[3];
+  std::vector<float> buf(3 * kNParams);
+  bool ok = std::fread(hdr, sizeof hdr, 1, f) == 1 && hdr[0] == 0x4255444553555231ull &&
+            hdr[1] == (unsigned long long)kNParams && std::fread(buf.data(), 4, buf.size(), f) == buf.size();
+  std::fclose(f);
+  if (!ok) return set_error(BUDE_ERR_ARG, "%s is not a surrogate checkpoint of this model", path);
+  cudaMemcpy(s.params.ptr, buf.data(), kNParams * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s.adam_m.ptr, buf.data() + kNParams, kNParams * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s.adam_v.ptr, buf.data() + 2 * kNParams, kNParams * 4, cudaMemcpyHostToDevice);
+  s.step = (long long)hdr[2];
+  return publish(c, s);
+}
+
+} // namespace bude
+
+using namespace bude;
+
+extern "C" {
+
+int bude_surrogate_init(bude_gpu_ctx *ctx, const bude_atom *protein, int32_t natpro, const bude_ffparams *forcefield,
+                        int32_t ntypes, float extent, float spacing, uint64_t seed) {
+  if (!ctx) return set_error(BUDE_ERR_ARG, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  return surrogate_init(*ctx, protein, natpro, forcefield, ntypes, extent, spacing, seed);
+}
+
+int bude_surrogate_train(bude_gpu_ctx *ctx, int32_t epochs, int32_t batch_poses, float lr, const float *labels,
+                         uint64_t seed, float *final_loss, float *train_ms) {
+  if (!ctx) return set_error(BUDE_ERR_ARG, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  return surrogate_train(*ctx, epochs, batch_poses, lr, labels, final_loss, train_ms, seed);
+}
+
+int bude_surrogate_score(bude_gpu_ctx *ctx, float *ms) {
+  if (!ctx) return set_error(BUDE_ERR_ARG, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  cudaEventRecord(ctx->ev0, ctx->stream);
+  int rc = surrogate_score_enqueue(*ctx, nullptr);
+  if (rc) return rc;
+  cudaEventRecord(ctx->ev1, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_error(e, "surrogate scoring");
+  if (ms) cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1);
+  return BUDE_OK;
+}
+
+int bude_surrogate_download(bude_gpu_ctx *ctx, float *scores, int64_t n) {
+  if (!ctx || (!scores && n > 0)) return set_error(BUDE_ERR_ARG, "NULL argument");
+  float *d = surrogate_scores(*ctx);
+  if (!d || !ctx->have_batch || n != ctx->batch_poses)
+    return set_error(BUDE_ERR_ARG, "no surrogate scores for %lld poses", (long long)n);
+  cudaError_t e = cudaMemcpy(scores, d, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "score download");
+}
+
+int bude_surrogate_gradient(bude_gpu_ctx *ctx, const int32_t *poses, int32_t n, const float *labels, float *grads,
+                            float *pred) {
+  if (!ctx || !poses || !labels || n <= 0) return set_error(BUDE_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  return surrogate_gradient(*ctx, poses, n, labels, grads, pred);
+}
+
+int bude_surrogate_features(bude_gpu_ctx *ctx, const int32_t *poses, int32_t n, float *features, int32_t *types) {
+  if (!ctx || !poses || !features || n <= 0) return set_error(BUDE_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  return surrogate_features(*ctx, poses, n, features, types);
+}
+
+int bude_surrogate_params(bude_gpu_ctx *ctx, float *out, const float *in, int64_t n) {
+  if (!ctx) return set_error(BUDE_ERR_ARG, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  return surrogate_io(*ctx, out, in, n);
+}
+
+int bude_surrogate_save(bude_gpu_ctx *ctx, const char *path) {
+  if (!ctx || !path) return set_error(BUDE_ERR_ARG, "NULL argument");
+  cudaSetDevice(ctx->device);
+  return surrogate_save(*ctx, path);
+}
+
+int bude_surrogate_load(bude_gpu_ctx *ctx, const char *path) {
+  if (!ctx || !path) return set_error(BUDE_ERR_ARG, "NULL argument");
+  cudaSetDevice(ctx->device);
+  return surrogate_load(*ctx, path);
+}
+
+} // extern "C"

@@ -1,0 +1,771 @@
+// surrogate_kernels.cuh -- the learned pre-screen: a per-ligand-atom MLP whose outputs are summed
+// per pose to approximate the exact pose energy.
+//
+// Model (all sizes fixed):
+//   features  x (32) = [type embedding (16) | transformed atom position * xyz_scale (3) |
+//                       13 protein-field channels sampled at the position]
+//   layers    z1 = W1 x + b1 (128), h1 = SiLU(z1); z2 = W2 h1 + b2, h2 = SiLU(z2);
+//             z3 = W3 h2 + b3, h3 = SiLU(z3); y = w4 . h3 + b4
+//   pose      E_pose = sum over the ligand's atoms of y
+// Weights W1..W3 and the embedding are BF16 on the device for the tensor cores (FP32 masters and
+// FP32 Adam state are kept beside them); activations are rounded to BF16 between layers; every
+// product accumulates in FP32 (mma.sync m16n8k16).  Weights are stored [out][in] (in contiguous),
+// so a layer's B fragments are plain ldmatrix loads; the backward pass uses transposed copies.
+//
+// The protein-field channels come from a grid precomputed once per protein (grid_kernel): for a
+// point x and protein atoms p (radius R_p, hphb h_p, elsc q_p, hbtype), distance r = |x - p|:
+//   c0..c3   sum_p relu(1 - r / (R + R_p))             probe radius R = 1.0, 1.5, 2.0, 2.5
+//   c4, c5   sum_p q_p   * sat(1 - (r - (1.75+R_p))/d)  d = 2, 4
+//   c6, c7   sum_p |q_p| * sat(1 - (r - (1.75+R_p))/d)  d = 2, 4
+//   c8       sum_{p: 'F'} q_p * sat(1 - (r - (1.75+R_p))/4)
+//   c9       sum_{p: h_p<0} h_p * sat(1 - (r - (1.75+R_p))/5.5)
+//   c10      sum_{p: h_p>0} h_p * sat(1 - (r - (1.75+R_p))/1)
+//   c11      sum_{p: h_p<0} h_p * sat(1 - (r - (1.75+R_p))/1)
+//   c12      min_p (r - R_p), clamped to [-3, 8]
+// i.e. the distance-dependent shapes of the steric, charge and desolvation terms of the exact
+// kernel for a few probe atoms, each scaled to unit standard deviation over the grid.  They are
+// sampled trilinearly.
+#pragma once
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "mlp.cuh"
+#include "ptx.cuh"
+
+namespace bude {
+
+constexpr int kFeat = 32;
+constexpr int kHid = 128;
+constexpr int kEmb = 16;
+constexpr int kGridCh = 13;
+constexpr int kMaxTypes = 64;
+constexpr int kRowsPerCta = 128; // 8 warps x 16 rows
+constexpr int kMlpThreads = 256;
+constexpr int kLdX = kFeat + 8;  // padded smem row strides (bf16 elements): conflict-free ldmatrix
+constexpr int kLdH = kHid + 8;
+
+// Parameters the forward kernels read (device pointers).
+struct MlpWeights {
+  const __nv_bfloat16 *emb; // [kMaxTypes][16]
+  const __nv_bfloat16 *w1;  // [128][32]
+  const __nv_bfloat16 *w2;  // [128][128]
+  const __nv_bfloat16 *w3;  // [128][128]
+  const float *b1, *b2, *b3, *w4, *b4; // [128] x 4, [1]
+};
+
+struct FieldGrid {
+  const float4 *data; // [nz][ny][nx][4] float4 = 16 channels, 13 used
+  float ox, oy, oz, inv_h;
+  int nx, ny, nz;
+  float xyz_scale;
+};
+
+// ---------------------------------------------------------------------------------------------
+// Field grid
+
+struct GridBuild {
+  const float4 *protein; // {x, y, z, type bits}
+  const bude_ffparams *ff;
+  int natpro;
+  float ox, oy, oz, h;
+  int nx, ny, nz;
+  float *out; // [voxels][16]
+};
+
+__global__ void __launch_bounds__(128) grid_kernel(GridBuild g) {
+  const long long nvox = (long long)g.nx * g.ny * g.nz;
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvox) return;
+  const int ix = (int)(v % g.nx);
+  const int iy = (int)((v / g.nx) % g.ny);
+  const int iz = (int)(v / ((long long)g.nx * g.ny));
+  const float x = g.ox + ix * g.h, y = g.oy + iy * g.h, z = g.oz + iz * g.h;
+  float c[kGridCh];
+#pragma unroll
+  for (int k = 0; k < kGridCh; ++k) c[k] = 0.f;
+  c[12] = 8.f;
+  for (int j = 0; j < g.natpro; ++j) {
+    const float4 p = __ldg(&g.protein[j]);
+    const bude_ffparams f = g.ff[__float_as_int(p.w)];
+    const float dx = x - p.x, dy = y - p.y, dz = z - p.z;
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    c[0] += fmaxf(0.f, 1.f - r / (1.0f + f.radius));
+    c[1] += fmaxf(0.f, 1.f - r / (1.5f + f.radius));
+    c[2] += fmaxf(0.f, 1.f - r / (2.0f + f.radius));
+    c[3] += fmaxf(0.f, 1.f - r / (2.5f + f.radius));
+    const float bb = r - (1.75f + f.radius);
+    const float s2 = __saturatef(1.f - bb * 0.5f), s4 = __saturatef(1.f - bb * 0.25f);
+    const float s55 = __saturatef(1.f - bb * (1.f / 5.5f)), s1 = __saturatef(1.f - bb);
+    c[4] += f.elsc * s2;
+    c[5] += f.elsc * s4;
+    c[6] += fabsf(f.elsc) * s2;
+    c[7] += fabsf(f.elsc) * s4;
+    if (f.hbtype == 70) c[8] += f.elsc * s4;
+    if (f.hphb < 0.f) {
+      c[9] += f.hphb * s55;
+      c[11] += f.hphb * s1;
+    } else if (f.hphb > 0.f) {
+      c[10] += f.hphb * s1;
+    }
+    c[12] = fminf(c[12], r - f.radius);
+  }
+  c[12] = fmaxf(c[12], -3.f);
+  float *o = g.out + v * 16;
+#pragma unroll
+  for (int k = 0; k < kGridCh; ++k) o[k] = c[k];
+  o[13] = o[14] = o[15] = 0.f;
+}
+
+// Divide every channel by its scale (channels 13..15 stay zero).
+__global__ void grid_scale_kernel(float *grid, long long nvox, const float *inv_scale) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvox * 16) return;
+  grid[i] *= inv_scale[i % 16];
+}
+
+// Trilinear sample of the 13 channels at a position (clamped to the grid).
+__device__ __forceinline__ void sample_field(const FieldGrid &g, float x, float y, float z, float (&c)[kGridCh]) {
+  float u = (x - g.ox) * g.inv_h, v = (y - g.oy) * g.inv_h, w = (z - g.oz) * g.inv_h;
+  u = fminf(fmaxf(u, 0.f), g.nx - 1.001f);
+  v = fminf(fmaxf(v, 0.f), g.ny - 1.001f);
+  w = fminf(fmaxf(w, 0.f), g.nz - 1.001f);
+  const int i0 = (int)u, j0 = (int)v, k0 = (int)w;
+  const float fu = u - i0, fv = v - j0, fw = w - k0;
+#pragma unroll
+  for (int k = 0; k < kGridCh; ++k) c[k] = 0.f;
+#pragma unroll
+  for (int corner = 0; corner < 8; ++corner) {
+    const int di = corner & 1, dj = (corner >> 1) & 1, dk = corner >> 2;
+    const float wt = (di ? fu : 1.f - fu) * (dj ? fv : 1.f - fv) * (dk ? fw : 1.f - fw);
+    const float4 *q = g.data + (((long long)(k0 + dk) * g.ny + (j0 + dj)) * g.nx + (i0 + di)) * 4;
+    const float4 a = __ldg(q), b = __ldg(q + 1), cc = __ldg(q + 2), d = __ldg(q + 3);
+    c[0] = fmaf(wt, a.x, c[0]);
+    c[1] = fmaf(wt, a.y, c[1]);
+    c[2] = fmaf(wt, a.z, c[2]);
+    c[3] = fmaf(wt, a.w, c[3]);
+    c[4] = fmaf(wt, b.x, c[4]);
+    c[5] = fmaf(wt, b.y, c[5]);
+    c[6] = fmaf(wt, b.z, c[6]);
+    c[7] = fmaf(wt, b.w, c[7]);
+    c[8] = fmaf(wt, cc.x, c[8]);
+    c[9] = fmaf(wt, cc.y, c[9]);
+    c[10] = fmaf(wt, cc.z, c[10]);
+    c[11] = fmaf(wt, cc.w, c[11]);
+    c[12] = fmaf(wt, d.x, c[12]);
+  }
+}
+
+// Features of one (pose, ligand atom) as 16 packed BF16 pairs.
+__device__ __forceinline__ void atom_features(const MlpWeights &W, const FieldGrid &g, float4 la, const float4 *xf,
+                                              uint32_t (&f)[kFeat / 2]) {
+  const float4 r0 = __ldg(xf), r1 = __ldg(xf + 1), r2 = __ldg(xf + 2);
+  const float x = r0.w + la.x * r0.x + la.y * r0.y + la.z * r0.z;
+  const float y = r1.w + la.x * r1.x + la.y * r1.y + la.z * r1.z;
+  const float z = r2.w + la.x * r2.x + la.y * r2.y + la.z * r2.z;
+  const int t = __float_as_int(la.w);
+  const uint4 *e = reinterpret_cast<const uint4 *>(W.emb + t * kEmb);
+  const uint4 e0 = __ldg(e), e1 = __ldg(e + 1);
+  f[0] = e0.x; f[1] = e0.y; f[2] = e0.z; f[3] = e0.w;
+  f[4] = e1.x; f[5] = e1.y; f[6] = e1.z; f[7] = e1.w;
+  float c[kGridCh];
+  sample_field(g, x, y, z, c);
+  f[8] = pack_bf16(x * g.xyz_scale, y * g.xyz_scale);
+  f[9] = pack_bf16(z * g.xyz_scale, c[0]);
+  f[10] = pack_bf16(c[1], c[2]);
+  f[11] = pack_bf16(c[3], c[4]);
+  f[12] = pack_bf16(c[5], c[6]);
+  f[13] = pack_bf16(c[7], c[8]);
+  f[14] = pack_bf16(c[9], c[10]);
+  f[15] = pack_bf16(c[11], c[12]);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Shared-memory copy of the BF16 weights (padded rows) and the FP32 vectors.
+
+struct MlpSmem {
+  __nv_bfloat16 w1[kHid * kLdX];
+  __nv_bfloat16 w2[kHid * kLdH];
+  __nv_bfloat16 w3[kHid * kLdH];
+  __nv_bfloat16 x[kRowsPerCta * kLdX];
+  float b1[kHid], b2[kHid], b3[kHid], w4[kHid];
+};
+
+__device__ __forceinline__ void load_weights(MlpSmem &s, const MlpWeights &W) {
+  for (int i = threadIdx.x; i < kHid * kFeat / 8; i += blockDim.x) {
+    const int o = i / (kFeat / 8), k8 = i % (kFeat / 8);
+    *reinterpret_cast<uint4 *>(&s.w1[o * kLdX + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(W.w1) + i);
+  }
+  for (int i = threadIdx.x; i < kHid * kHid / 8; i += blockDim.x) {
+    const int o = i / (kHid / 8), k8 = i % (kHid / 8);
+    *reinterpret_cast<uint4 *>(&s.w2[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(W.w2) + i);
+    *reinterpret_cast<uint4 *>(&s.w3[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(W.w3) + i);
+  }
+  for (int i = threadIdx.x; i < kHid; i += blockDim.x) {
+    s.b1[i] = W.b1[i];
+    s.b2[i] = W.b2[i];
+    s.b3[i] = W.b3[i];
+    s.w4[i] = W.w4[i];
+  }
+}
+
+// One 16-row x 128-column layer: acc = A * W^T, A given as 16x16 fragments for NK k-steps.
+template <int NK, int LDW>
+__device__ __forceinline__ void layer_mma(float (&acc)[16][4], const uint32_t (&a)[NK][4],
+                                          const __nv_bfloat16 *w) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+  for (int kk = 0; kk < NK; ++kk) {
+#pragma unroll
+    for (int jp = 0; jp < 8; ++jp) { // n-tiles 2jp, 2jp+1
+      uint32_t b[4];
+      const int row = jp * 16 + (lane & 7) + ((lane >> 4) << 3);
+      const int col = kk * 16 + ((lane >> 3) & 1) * 8;
+      ldsm_x4(b, w + row * LDW + col);
+      mma_bf16(acc[2 * jp], a[kk], b[0], b[1]);
+      mma_bf16(acc[2 * jp + 1], a[kk], b[2], b[3]);
+    }
+  }
+}
+
+// bias + SiLU on a layer's accumulators and repack them as the next layer's A fragments;
+// z (optional) receives the pre-activations as BF16 pairs in accumulator layout.
+__device__ __forceinline__ void act_to_frags(float (&acc)[16][4], const float *bias, uint32_t (&a)[8][4],
+                                             uint32_t (*z)[2]) {
+  const int t = threadIdx.x & 3;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const float bl = bias[j * 8 + 2 * t], bh = bias[j * 8 + 2 * t + 1];
+    const float z0 = acc[j][0] + bl, z1 = acc[j][1] + bh, z2 = acc[j][2] + bl, z3 = acc[j][3] + bh;
+    if (z) {
+      z[j][0] = pack_bf16(z0, z1);
+      z[j][1] = pack_bf16(z2, z3);
+    }
+    const uint32_t lo = pack_bf16(silu(z0), silu(z1)); // row g
+    const uint32_t hi = pack_bf16(silu(z2), silu(z3)); // row g + 8
+    const int kk = j >> 1;
+    if ((j & 1) == 0) {
+      a[kk][0] = lo;
+      a[kk][1] = hi;
+    } else {
+      a[kk][2] = lo;
+      a[kk][3] = hi;
+    }
+  }
+}
+
+// Final layer on A-fragment-packed h3: y for rows g and g+8 (full dot after the quad reduce).
+__device__ __forceinline__ float2 last_layer(const uint32_t (&h3)[8][4], const float *w4) {
+  const int t = threadIdx.x & 3;
+  float y0 = 0.f, y1 = 0.f;
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk) {
+    const int c0 = kk * 16 + 2 * t, c1 = c0 + 8;
+    float2 v;
+    v = unpack_bf16(h3[kk][0]);
+    y0 = fmaf(v.x, w4[c0], fmaf(v.y, w4[c0 + 1], y0));
+    v = unpack_bf16(h3[kk][2]);
+    y0 = fmaf(v.x, w4[c1], fmaf(v.y, w4[c1 + 1], y0));
+    v = unpack_bf16(h3[kk][1]);
+    y1 = fmaf(v.x, w4[c0], fmaf(v.y, w4[c0 + 1], y1));
+    v = unpack_bf16(h3[kk][3]);
+    y1 = fmaf(v.x, w4[c1], fmaf(v.y, w4[c1 + 1], y1));
+  }
+  y0 += __shfl_xor_sync(0xffffffffu, y0, 1);
+  y0 += __shfl_xor_sync(0xffffffffu, y0, 2);
+  y1 += __shfl_xor_sync(0xffffffffu, y1, 1);
+  y1 += __shfl_xor_sync(0xffffffffu, y1, 2);
+  return make_float2(y0, y1);
+}
+
+// Load a warp's 16 rows of the smem feature tile as layer-1 A fragments.
+__device__ __forceinline__ void x_frags(const __nv_bfloat16 *xs, int row0, uint32_t (&a)[2][4]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int kk = 0; kk < 2; ++kk) {
+    const int row = row0 + (lane & 7) + ((lane >> 3) & 1) * 8;
+    const int col = kk * 16 + (lane >> 4) * 8;
+    ldsm_x4(a[kk], xs + row * kLdX + col);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Inference: one block per item (ligand, block of up to 128 poses); features are built per ligand
+// atom into shared memory and run through the MLP by 8 warps of 16 poses each.
+
+struct ScoreArgs {
+  MlpWeights W;
+  FieldGrid g;
+  const float4 *ligands; // concatenated ligand atoms
+  const float4 *xform;   // [poses][3]
+  const int4 *items;     // {first ligand atom, natlig, first pose, pose count}
+  float *scores;         // per pose
+  int n_items;
+};
+
+__global__ void __launch_bounds__(kMlpThreads) score_kernel(const ScoreArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  MlpSmem &s = *reinterpret_cast<MlpSmem *>(smem_raw);
+  load_weights(s, a.W);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
+  for (int item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+    const int4 it = __ldg(&a.items[item]);
+    float e0 = 0.f, e1 = 0.f; // rows warp*16 + g and + 8
+    for (int il = 0; il < it.y; ++il) {
+      __syncthreads(); // previous tile consumed (and weights loaded)
+      const float4 la = __ldg(&a.ligands[it.x + il]);
+      if (threadIdx.x < kRowsPerCta) {
+        const int r = threadIdx.x;
+        const int pose = it.z + min(r, it.w - 1);
+        uint32_t f[kFeat / 2];
+        atom_features(a.W, a.g, la, a.xform + (long long)pose * 3, f);
+        uint4 *dst = reinterpret_cast<uint4 *>(&s.x[r * kLdX]);
+        dst[0] = make_uint4(f[0], f[1], f[2], f[3]);
+        dst[1] = make_uint4(f[4], f[5], f[6], f[7]);
+        dst[2] = make_uint4(f[8], f[9], f[10], f[11]);
+        dst[3] = make_uint4(f[12], f[13], f[14], f[15]);
+      }
+      __syncthreads();
+      uint32_t ax[2][4], h[8][4];
+      float acc[16][4];
+      x_frags(s.x, warp * 16, ax);
+      layer_mma<2, kLdX>(acc, ax, s.w1);
+      act_to_frags(acc, s.b1, h, nullptr);
+      layer_mma<8, kLdH>(acc, h, s.w2);
+      act_to_frags(acc, s.b2, h, nullptr);
+      layer_mma<8, kLdH>(acc, h, s.w3);
+      act_to_frags(acc, s.b3, h, nullptr);
+      const float2 y = last_layer(h, s.w4);
+      e0 += y.x;
+      e1 += y.y;
+    }
+    if ((lane & 3) == 0) {
+      const float nb4 = it.y * __ldg(a.W.b4);
+      const int r0 = warp * 16 + g, r1 = r0 + 8;
+      if (r0 < it.w) a.scores[it.z + r0] = e0 + nb4;
+      if (r1 < it.w) a.scores[it.z + r1] = e1 + nb4;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Training.  A batch is a list of poses; its rows (pose, ligand atom) are laid out pose by pose.
+
+struct RowMap {
+  const int *pose;    // global pose index per batch pose
+  const int *row_off; // batch poses + 1 row offsets
+  const int *lig_first, *lig_n; // per global pose: first atom and atom count of its ligand
+  int nposes;
+};
+
+// One warp per batch pose writes the features (and types) of its rows.
+__global__ void __launch_bounds__(256) train_features_kernel(MlpWeights W, FieldGrid g, const float4 *ligands,
+                                                             const float4 *xform, RowMap m, __nv_bfloat16 *X,
+                                                             int *row_type) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= m.nposes) return;
+  const int p = m.pose[i];
+  const int first = m.lig_first[p], n = m.lig_n[p], row0 = m.row_off[i];
+  for (int a = lane; a < n; a += 32) {
+    const float4 la = __ldg(&ligands[first + a]);
+    uint32_t f[kFeat / 2];
+    atom_features(W, g, la, xform + (long long)p * 3, f);
+    uint4 *dst = reinterpret_cast<uint4 *>(X + (long long)(row0 + a) * kFeat);
+    dst[0] = make_uint4(f[0], f[1], f[2], f[3]);
+    dst[1] = make_uint4(f[4], f[5], f[6], f[7]);
+    dst[2] = make_uint4(f[8], f[9], f[10], f[11]);
+    dst[3] = make_uint4(f[12], f[13], f[14], f[15]);
+    row_type[row0 + a] = __float_as_int(la.w);
+  }
+}
+
+// Forward over rows: saves z1, z2, z3 (BF16, [rows][128]) and y per row.
+__global__ void __launch_bounds__(kMlpThreads) train_forward_kernel(MlpWeights W, const __nv_bfloat16 *X, int rows,
+                                                                    __nv_bfloat16 *Z1, __nv_bfloat16 *Z2,
+                                                                    __nv_bfloat16 *Z3, float *y) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  MlpSmem &s = *reinterpret_cast<MlpSmem *>(smem_raw);
+  load_weights(s, W);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  for (int tile = blockIdx.x; tile * kRowsPerCta < rows; tile += gridDim.x) {
+    const int base = tile * kRowsPerCta;
+    __syncthreads();
+    for (int i = threadIdx.x; i < kRowsPerCta * kFeat / 8; i += blockDim.x) {
+      const int r = i / (kFeat / 8), k8 = i % (kFeat / 8);
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (base + r < rows) v = *reinterpret_cast<const uint4 *>(X + (long long)(base + r) * kFeat + k8 * 8);
+      *reinterpret_cast<uint4 *>(&s.x[r * kLdX + k8 * 8]) = v;
+    }
+    __syncthreads();
+    uint32_t ax[2][4], h[8][4], z[16][2];
+    float acc[16][4];
+    const int r0 = base + warp * 16 + g, r1 = r0 + 8;
+    auto store_z = [&](__nv_bfloat16 *Z) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        if (r0 < rows) *reinterpret_cast<uint32_t *>(Z + (long long)r0 * kHid + j * 8 + 2 * t) = z[j][0];
+        if (r1 < rows) *reinterpret_cast<uint32_t *>(Z + (long long)r1 * kHid + j * 8 + 2 * t) = z[j][1];
+      }
+    };
+    x_frags(s.x, warp * 16, ax);
+    layer_mma<2, kLdX>(acc, ax, s.w1);
+    act_to_frags(acc, s.b1, h, z);
+    store_z(Z1);
+    layer_mma<8, kLdH>(acc, h, s.w2);
+    act_to_frags(acc, s.b2, h, z);
+    store_z(Z2);
+    layer_mma<8, kLdH>(acc, h, s.w3);
+    act_to_frags(acc, s.b3, h, z);
+    store_z(Z3);
+    const float2 yy = last_layer(h, s.w4);
+    if (t == 0) {
+      if (r0 < rows) y[r0] = yy.x;
+      if (r1 < rows) y[r1] = yy.y;
+    }
+  }
+}
+
+// Per batch pose: prediction = sum of its rows' y + natlig * b4; loss on the compressed scale
+// c(E) = S * asinh(E / S); dy (per row) = dLoss/dprediction.  loss_out[i] = the pose's squared
+// error (summed on the host, deterministic).
+constexpr float kLossScale = 20.f;
+
+__global__ void train_loss_kernel(RowMap m, const float *y, const float *b4, const float *labels, float *pred,
+                                  float *loss_out, float *dy, float inv_batch) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.nposes) return;
+  const int p = m.pose[i];
+  const int row0 = m.row_off[i], n = m.row_off[i + 1] - row0;
+  float s = 0.f;
+  for (int a = 0; a < n; ++a) s += y[row0 + a];
+  s += n * b4[0];
+  pred[i] = s;
+  const float cs = kLossScale * asinhf(s / kLossScale), ce = kLossScale * asinhf(labels[p] / kLossScale);
+  const float d = cs - ce;
+  loss_out[i] = d * d;
+  const float grad = 2.f * d * rsqrtf(1.f + (s / kLossScale) * (s / kLossScale)) * inv_batch;
+  for (int a = 0; a < n; ++a) dy[row0 + a] = grad;
+}
+
+// Backward through the layers for a tile of rows: writes dz3, dz2, dz1 (BF16) for the weight
+// gradients, and per block: d w4 / d b4 partials, bias partials and embedding partials (each
+// summed in a fixed order, so the whole backward pass is deterministic).
+struct BwdArgs {
+  const __nv_bfloat16 *w1t; // [32][128]  (W1 transposed: in x out)
+  const __nv_bfloat16 *w2t; // [128][128]
+  const __nv_bfloat16 *w3t; // [128][128]
+  const float *w4;
+  const __nv_bfloat16 *Z1, *Z2, *Z3;
+  const float *dy;
+  const int *row_type;
+  int rows;
+  __nv_bfloat16 *dZ1, *dZ2, *dZ3;
+  float *part_w4;  // [blocks][128]
+  float *part_b;   // [blocks][4][128]  (b1, b2, b3, b4 in slot 3 col 0)
+  float *part_emb; // [blocks][kMaxTypes][16]
+};
+
+struct BwdSmem {
+  __nv_bfloat16 w2t[kHid * kLdH];
+  __nv_bfloat16 w3t[kHid * kLdH];
+  __nv_bfloat16 w1t[kFeat * kLdH];
+  float w4[kHid];
+  float red[8][kHid];        // per-warp column sums
+  float demb[kRowsPerCta][kEmb];
+  int type[kRowsPerCta];
+  float emb_acc[kMaxTypes][kEmb];
+};
+
+__global__ void __launch_bounds__(kMlpThreads) train_backward_kernel(BwdArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  BwdSmem &s = *reinterpret_cast<BwdSmem *>(smem_raw);
+  for (int i = threadIdx.x; i < kHid * kHid / 8; i += blockDim.x) {
+    const int o = i / (kHid / 8), k8 = i % (kHid / 8);
+    *reinterpret_cast<uint4 *>(&s.w2t[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(a.w2t) + i);
+    *reinterpret_cast<uint4 *>(&s.w3t[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(a.w3t) + i);
+  }
+  for (int i = threadIdx.x; i < kFeat * kHid / 8; i += blockDim.x) {
+    const int o = i / (kHid / 8), k8 = i % (kHid / 8);
+    *reinterpret_cast<uint4 *>(&s.w1t[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(a.w1t) + i);
+  }
+  for (int i = threadIdx.x; i < kHid; i += blockDim.x) s.w4[i] = a.w4[i];
+  for (int i = threadIdx.x; i < kMaxTypes * kEmb; i += blockDim.x) (&s.emb_acc[0][0])[i] = 0.f;
+  __syncthreads(); // the staged weights are read by every warp below
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  // Block-level partials accumulate in registers of threads < 128 (one column each).
+  float acc_b[4] = {0.f, 0.f, 0.f, 0.f};
+  float acc_w4 = 0.f;
+
+  // Column sums of a warp's 16 x 128 BF16-pair values (v[j][0] row g, v[j][1] row g+8) into
+  // s.red[warp][col]; values are first summed over the 8 row groups with shuffles in a fixed order.
+  auto colsum = [&](const float (&v)[16][4]) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      float c0 = v[j][0] + v[j][2], c1 = v[j][1] + v[j][3];
+#pragma unroll
+      for (int off = 4; off < 32; off <<= 1) {
+        c0 += __shfl_xor_sync(0xffffffffu, c0, off);
+        c1 += __shfl_xor_sync(0xffffffffu, c1, off);
+      }
+      if (g == 0) {
+        s.red[warp][j * 8 + 2 * t] = c0;
+        s.red[warp][j * 8 + 2 * t + 1] = c1;
+      }
+    }
+  };
+  auto fold = [&](float &dst) { // sum the 8 warps' column sums in order (threads < 128)
+    __syncthreads();
+    if (threadIdx.x < kHid) {
+      float v = 0.f;
+      for (int w = 0; w < 8; ++w) v += s.red[w][threadIdx.x];
+      dst += v;
+    }
+    __syncthreads();
+  };
+
+  for (int tile = blockIdx.x; tile * kRowsPerCta < a.rows; tile += gridDim.x) {
+    const int base = tile * kRowsPerCta;
+    const int r0 = base + warp * 16 + g, r1 = r0 + 8;
+    const bool v0 = r0 < a.rows, v1 = r1 < a.rows;
+    const float dy0 = v0 ? a.dy[r0] : 0.f, dy1 = v1 ? a.dy[r1] : 0.f;
+    auto zload = [&](const __nv_bfloat16 *Z, int j, float (&z)[4]) {
+      const float2 lo = v0 ? unpack_bf16(*reinterpret_cast<const uint32_t *>(Z + (long long)r0 * kHid + j * 8 + 2 * t))
+                           : make_float2(0.f, 0.f);
+      const float2 hi = v1 ? unpack_bf16(*reinterpret_cast<const uint32_t *>(Z + (long long)r1 * kHid + j * 8 + 2 * t))
+                           : make_float2(0.f, 0.f);
+      z[0] = lo.x; z[1] = lo.y; z[2] = hi.x; z[3] = hi.y;
+    };
+    auto dz_store = [&](__nv_bfloat16 *dZ, int j, const float (&d)[4]) {
+      if (v0) *reinterpret_cast<uint32_t *>(dZ + (long long)r0 * kHid + j * 8 + 2 * t) = pack_bf16(d[0], d[1]);
+      if (v1) *reinterpret_cast<uint32_t *>(dZ + (long long)r1 * kHid + j * 8 + 2 * t) = pack_bf16(d[2], d[3]);
+    };
+    // Layer 4 -> dz3 (and the w4 gradient dy * h3).
+    float dz[16][4], cs[16][4];
+    uint32_t A[8][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      float z[4];
+      zload(a.Z3, j, z);
+      const int c0 = j * 8 + 2 * t;
+      dz[j][0] = dy0 * s.w4[c0] * silu_grad(z[0]);
+      dz[j][1] = dy0 * s.w4[c0 + 1] * silu_grad(z[1]);
+      dz[j][2] = dy1 * s.w4[c0] * silu_grad(z[2]);
+      dz[j][3] = dy1 * s.w4[c0 + 1] * silu_grad(z[3]);
+      cs[j][0] = dy0 * silu(z[0]);
+      cs[j][1] = dy0 * silu(z[1]);
+      cs[j][2] = dy1 * silu(z[2]);
+      cs[j][3] = dy1 * silu(z[3]);
+    }
+    colsum(cs);
+    fold(acc_w4);
+    // b4 gradient: sum of dy over the tile's rows (slot 3, column 0), in a fixed order.
+    {
+      float d = (t == 0) ? dy0 + dy1 : 0.f;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
+      if (lane == 0) s.red[warp][0] = d;
+      for (int j = 1; j < 16 && lane == 0; ++j) s.red[warp][j] = 0.f;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        float v = 0.f;
+        for (int w = 0; w < 8; ++w) v += s.red[w][0];
+        acc_b[3] += v;
+      }
+      __syncthreads();
+    }
+    // dz3 -> BF16 A fragments, store, bias-3 partial.
+    auto to_frags = [&](const float (&d)[16][4], __nv_bfloat16 *dZ, float &bacc) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        dz_store(dZ, j, d[j]);
+        const uint32_t lo = pack_bf16(d[j][0], d[j][1]), hi = pack_bf16(d[j][2], d[j][3]);
+        if ((j & 1) == 0) {
+          A[j >> 1][0] = lo;
+          A[j >> 1][1] = hi;
+        } else {
+          A[j >> 1][2] = lo;
+          A[j >> 1][3] = hi;
+        }
+      }
+      colsum(d);
+      fold(bacc);
+    };
+    to_frags(dz, a.dZ3, acc_b[2]);
+    // dh2 = dz3 W3 ; dz2 = dh2 * silu'(z2)
+    float acc[16][4];
+    layer_mma<8, kLdH>(acc, A, s.w3t);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      float z[4];
+      zload(a.Z2, j, z);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * silu_grad(z[q]);
+    }
+    to_frags(dz, a.dZ2, acc_b[1]);
+    // dh1 = dz2 W2 ; dz1 = dh1 * silu'(z1)
+    layer_mma<8, kLdH>(acc, A, s.w2t);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      float z[4];
+      zload(a.Z1, j, z);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * silu_grad(z[q]);
+    }
+    to_frags(dz, a.dZ1, acc_b[0]);
+    // dx (embedding columns 0..15) = dz1 W1: two n-tiles of W1^T rows 0..15.
+    {
+      float dx[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        uint32_t b[4];
+        const int row = (lane & 7) + ((lane >> 4) << 3);
+        const int col = kk * 16 + ((lane >> 3) & 1) * 8;
+        ldsm_x4(b, s.w1t + row * kLdH + col);
+        mma_bf16(dx[0], A[kk], b[0], b[1]);
+        mma_bf16(dx[1], A[kk], b[2], b[3]);
+      }
+      const int lr0 = warp * 16 + g, lr1 = lr0 + 8;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        s.demb[lr0][j * 8 + 2 * t] = v0 ? dx[j][0] : 0.f;
+        s.demb[lr0][j * 8 + 2 * t + 1] = v0 ? dx[j][1] : 0.f;
+        s.demb[lr1][j * 8 + 2 * t] = v1 ? dx[j][2] : 0.f;
+        s.demb[lr1][j * 8 + 2 * t + 1] = v1 ? dx[j][3] : 0.f;
+      }
+      if (t == 0) {
+        s.type[lr0] = v0 ? a.row_type[r0] : 0;
+        s.type[lr1] = v1 ? a.row_type[r1] : 0;
+      }
+      __syncthreads();
+      if (threadIdx.x < kEmb) { // thread j owns embedding column j: rows in order
+        for (int r = 0; r < kRowsPerCta; ++r) s.emb_acc[s.type[r]][threadIdx.x] += s.demb[r][threadIdx.x];
+      }
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x < kHid) {
+    a.part_w4[(long long)blockIdx.x * kHid + threadIdx.x] = acc_w4;
+    for (int l = 0; l < 4; ++l) a.part_b[((long long)blockIdx.x * 4 + l) * kHid + threadIdx.x] = acc_b[l];
+  }
+  for (int i = threadIdx.x; i < kMaxTypes * kEmb; i += blockDim.x)
+    a.part_emb[(long long)blockIdx.x * kMaxTypes * kEmb + i] = (&s.emb_acc[0][0])[i];
+}
+
+// Weight gradient partials of one layer: part[chunk] = dZ^T H over `chunk_rows` rows, with
+// H = SiLU(Zin) (or the features X for layer 1, kin = 32).  8 warps x 16 output rows.
+struct WgradArgs {
+  const __nv_bfloat16 *dZ;  // [rows][128]
+  const __nv_bfloat16 *Hin; // [rows][KIN]: pre-activations (apply SiLU) or features
+  int apply_silu;
+  int rows;
+  int chunk_rows; // multiple of 16
+  float *part;    // [chunks][128][kin]
+};
+
+struct WgradSmem {
+  __nv_bfloat16 dz[16 * kLdH];
+  __nv_bfloat16 h[16 * kLdH];
+};
+
+template <int KIN>
+__global__ void __launch_bounds__(kMlpThreads) wgrad_kernel(WgradArgs a) {
+  __shared__ __align__(16) WgradSmem s;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  constexpr int nt = KIN / 8; // n-tiles of the output row
+  float acc[16][4];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  const int r_begin = blockIdx.x * a.chunk_rows;
+  const int r_end = min(a.rows, r_begin + a.chunk_rows);
+  for (int r = r_begin; r < r_end; r += 16) {
+    __syncthreads();
+    // stage 16 rows of dZ (128 wide) and of H (kin wide)
+    for (int i = threadIdx.x; i < 16 * kHid / 8; i += blockDim.x) {
+      const int rr = i / (kHid / 8), k8 = i % (kHid / 8);
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (r + rr < r_end) v = *reinterpret_cast<const uint4 *>(a.dZ + (long long)(r + rr) * kHid + k8 * 8);
+      *reinterpret_cast<uint4 *>(&s.dz[rr * kLdH + k8 * 8]) = v;
+    }
+    for (int i = threadIdx.x; i < 16 * KIN / 8; i += blockDim.x) {
+      const int rr = i / (KIN / 8), k8 = i % (KIN / 8);
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (r + rr < r_end) {
+        v = *reinterpret_cast<const uint4 *>(a.Hin + (long long)(r + rr) * KIN + k8 * 8);
+        if (a.apply_silu) {
+          uint32_t *w = reinterpret_cast<uint32_t *>(&v);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float2 f = unpack_bf16(w[q]);
+            w[q] = pack_bf16(silu(f.x), silu(f.y));
+          }
+        }
+      }
+      *reinterpret_cast<uint4 *>(&s.h[rr * kLdH + k8 * 8]) = v;
+    }
+    __syncthreads();
+    // A (m = out row, k = data row) = dZ^T: transposed 8x8 loads of dz[r][o].
+    uint32_t af[4];
+    {
+      const int q = lane >> 3;
+      const int row = (lane & 7) + ((q >> 1) << 3);
+      const int col = warp * 16 + ((q & 1) << 3);
+      ldsm_x4_trans(af, s.dz + row * kLdH + col);
+    }
+#pragma unroll
+    for (int jp = 0; jp < nt / 2; ++jp) {
+      uint32_t b[4];
+      const int q = lane >> 3;
+      const int row = (lane & 7) + ((q & 1) << 3);
+      const int col = jp * 16 + ((q >> 1) << 3);
+      ldsm_x4_trans(b, s.h + row * kLdH + col);
+      mma_bf16(acc[2 * jp], af, b[0], b[1]);
+      mma_bf16(acc[2 * jp + 1], af, b[2], b[3]);
+    }
+  }
+  float *out = a.part + (long long)blockIdx.x * kHid * KIN;
+  const int o0 = warp * 16 + g, o1 = o0 + 8;
+#pragma unroll
+  for (int j = 0; j < nt; ++j) {
+    out[o0 * KIN + j * 8 + 2 * t] = acc[j][0];
+    out[o0 * KIN + j * 8 + 2 * t + 1] = acc[j][1];
+    out[o1 * KIN + j * 8 + 2 * t] = acc[j][2];
+    out[o1 * KIN + j * 8 + 2 * t + 1] = acc[j][3];
+  }
+}
+
+// grad[i] = sum over parts of part[p][i], in part order.
+__global__ void reduce_parts_kernel(const float *part, int nparts, long long n, long long stride, float *grad) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float v = 0.f;
+  for (int p = 0; p < nparts; ++p) v += part[p * stride + i];
+  grad[i] = v;
+}
+
+// Adam on the FP32 masters; bias-corrected step size lr_t precomputed on the host.
+__global__ void adam_kernel(float *w, float *m, float *v, const float *grad, long long n, float lr_t, float b1,
+                            float b2, float eps) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gr = grad[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gr;
+  const float vi = b2 * v[i] + (1.f - b2) * gr * gr;
+  m[i] = mi;
+  v[i] = vi;
+  w[i] -= lr_t * mi / (sqrtf(vi) + eps);
+}
+
+// BF16 copies of a [rows][cols] FP32 master: plain (optional) and transposed (optional).
+__global__ void publish_kernel(const float *w, int rows, int cols, __nv_bfloat16 *plain, __nv_bfloat16 *trans) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows * cols) return;
+  const int r = i / cols, c = i % cols;
+  const __nv_bfloat16 b = __float2bfloat16_rn(w[i]);
+  if (plain) plain[i] = b;
+  if (trans) trans[c * rows + r] = b;
+}
+
+} // namespace bude

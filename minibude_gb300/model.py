@@ -16,7 +16,7 @@ from typing import List, Optional, Sequence, Tuple
 import numpy as np
 
 from . import capi
-from .capi import BudeLaunchCfg, check, fptr, ptr
+from .capi import SURROGATE_NPARAMS, BudeLaunchCfg, BudeScreenCfg, BudeScreenStats, check, fptr, ptr
 from .deck import ATOM_DTYPE, FF_DTYPE, Deck
 
 
@@ -154,6 +154,73 @@ class GpuContext:
         out = np.zeros(self.batch_poses, np.float32)
         check(self._lib.bude_gpu_download_batch(self.handle, fptr(out), self.batch_poses))
         return out
+
+    # -- learned pre-screen --------------------------------------------------------------------
+    def surrogate_init(self, protein, forcefield, extent: float = 11.0, spacing: float = 0.4, seed: int = 0):
+        protein, ff = _atoms(protein), _ff(forcefield)
+        check(self._lib.bude_surrogate_init(self.handle, ptr(protein), protein.size, ptr(ff), ff.size, extent, spacing,
+                                            seed))
+
+    def surrogate_train(self, epochs: int, batch_poses: int = 8192, lr: float = 1e-3, labels=None, seed: int = 0):
+        """Train on the uploaded batch; returns (last-epoch mean loss, GPU ms)."""
+        lab = None if labels is None else np.ascontiguousarray(labels, np.float32)
+        loss, ms = ctypes.c_float(), ctypes.c_float()
+        check(self._lib.bude_surrogate_train(self.handle, epochs, batch_poses, lr, ptr(lab), seed, ctypes.byref(loss),
+                                             ctypes.byref(ms)))
+        return loss.value, ms.value
+
+    def surrogate_score(self) -> float:
+        ms = ctypes.c_float()
+        check(self._lib.bude_surrogate_score(self.handle, ctypes.byref(ms)))
+        return ms.value
+
+    def surrogate_download(self) -> np.ndarray:
+        out = np.zeros(self.batch_poses, np.float32)
+        check(self._lib.bude_surrogate_download(self.handle, fptr(out), self.batch_poses))
+        return out
+
+    def surrogate_gradient(self, poses, labels):
+        poses = np.ascontiguousarray(poses, np.int32)
+        labels = np.ascontiguousarray(labels, np.float32)
+        grads = np.zeros(SURROGATE_NPARAMS, np.float32)
+        pred = np.zeros(poses.size, np.float32)
+        check(self._lib.bude_surrogate_gradient(self.handle, ptr(poses), poses.size, ptr(labels), fptr(grads),
+                                                fptr(pred)))
+        return grads, pred
+
+    def surrogate_features(self, poses, rows: int):
+        poses = np.ascontiguousarray(poses, np.int32)
+        X = np.zeros((rows, 32), np.float32)
+        types = np.zeros(rows, np.int32)
+        check(self._lib.bude_surrogate_features(self.handle, ptr(poses), poses.size, fptr(X), ptr(types)))
+        return X, types
+
+    def surrogate_params(self, new=None) -> np.ndarray:
+        out = np.zeros(SURROGATE_NPARAMS, np.float32)
+        src = None if new is None else np.ascontiguousarray(new, np.float32)
+        check(self._lib.bude_surrogate_params(self.handle, fptr(out), fptr(src), SURROGATE_NPARAMS))
+        return out
+
+    def surrogate_save(self, path: str):
+        check(self._lib.bude_surrogate_save(self.handle, path.encode()))
+
+    def surrogate_load(self, path: str):
+        check(self._lib.bude_surrogate_load(self.handle, path.encode()))
+
+    # -- screening -------------------------------------------------------------------------------
+    def screen(self, exact_cfg: BudeLaunchCfg, top_frac: float = 0.02, audit_frac: float = 0.005,
+               audit_tol: float = 0.05, seed: int = 1) -> dict:
+        cfg = BudeScreenCfg(top_frac, audit_frac, audit_tol, seed, exact_cfg)
+        st = BudeScreenStats()
+        check(self._lib.bude_screen_run(self.handle, ctypes.byref(cfg), ctypes.byref(st)))
+        return st.as_dict()
+
+    def screen_download(self, nligands: int):
+        final = np.zeros(self.batch_poses, np.float32)
+        rescored = np.zeros(self.batch_poses, np.uint8)
+        err = np.zeros(max(nligands, 1), np.float32)
+        check(self._lib.bude_screen_download(self.handle, fptr(final), ptr(rescored), fptr(err), self.batch_poses))
+        return final, rescored.astype(bool), err[:nligands]
 
     def launch_count(self) -> int:
         n = ctypes.c_int64()

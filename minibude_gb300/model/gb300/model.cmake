@@ -20,6 +20,8 @@ macro(setup)
             ${GB300_ROOT}/minibude_gb300/csrc/bude_gb300.cu
             ${GB300_ROOT}/minibude_gb300/csrc/autotune.cu
             ${GB300_ROOT}/minibude_gb300/csrc/batch.cu
+            ${GB300_ROOT}/minibude_gb300/csrc/surrogate.cu
+            ${GB300_ROOT}/minibude_gb300/csrc/screen.cu
             ${GB300_ROOT}/minibude_gb300/csrc/noalloc.cu
             ${GB300_ROOT}/minibude_gb300/csrc/arch_probe.cu)
     target_include_directories(bude_gb300 PUBLIC ${GB300_ROOT}/include)

@@ -1,0 +1,168 @@
+"""The learned pre-screen: MLP forward and gradients against a plain PyTorch FP32 reference,
+training behaviour, checkpoints, and the screening pipeline's invariants (the exact kernel judges
+every pose it reports)."""
+import numpy as np
+import pytest
+
+import surrogate_ref as ref
+from minibude_gb300 import SMALL, BatchSpec, synthetic_batch, synthetic_deck
+from minibude_gb300.capi import BUDE_ERR_ARG, BudeError
+from minibude_gb300.model import GpuContext, launch_cfg
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def small_protein():
+    d = synthetic_deck(SMALL, 0, 1)
+    return d.protein, d.forcefield
+
+
+@pytest.fixture(scope="module")
+def setup(built_library):
+    protein, ff = small_protein()
+    batch = synthetic_batch(BatchSpec("t", 10, 16, 64, 200, 600), protein, ff, 5)
+    ctx = GpuContext(0)
+    ctx.upload_batch(batch)
+    ctx.surrogate_init(protein, ff, extent=11.0, spacing=0.4, seed=3)
+    yield ctx, batch
+    ctx.close()
+
+
+def counts_of(batch, poses):
+    lo = batch.pose_offsets()
+    lig = np.searchsorted(lo, poses, side="right") - 1
+    return np.array([len(batch.ligands[l]) for l in lig])
+
+
+def test_forward_matches_torch(setup):
+    ctx, batch = setup
+    ctx.surrogate_score()
+    got = ctx.surrogate_download()
+    poses = np.arange(0, batch.total_poses, 37, dtype=np.int32)
+    cnt = counts_of(batch, poses)
+    X, types = ctx.surrogate_features(poses, int(cnt.sum()))
+    P = ref.split(ctx.surrogate_params(), torch)
+    with torch.no_grad():
+        want = ref.pose_sums(torch, ref.row_outputs(torch, P, X, types), cnt).numpy()
+    scale = np.maximum(np.abs(want), 1.0)
+    assert np.max(np.abs(got[poses] - want) / scale) < 2e-2
+
+
+def test_gradient_matches_torch_autograd(setup):
+    ctx, batch = setup
+    rng = np.random.default_rng(0)
+    labels = rng.normal(50.0, 80.0, batch.total_poses).astype(np.float32)
+    poses = rng.choice(batch.total_poses, 300, replace=False).astype(np.int32)
+    grads, pred = ctx.surrogate_gradient(poses, labels)
+    cnt = counts_of(batch, poses)
+    X, types = ctx.surrogate_features(poses, int(cnt.sum()))
+    P = ref.split(ctx.surrogate_params(), torch, requires_grad=True)
+    tp = ref.pose_sums(torch, ref.row_outputs(torch, P, X, types), cnt)
+    L = ref.loss(torch, tp, labels[poses])
+    L.backward()
+    assert np.max(np.abs(pred - tp.detach().numpy()) / np.maximum(np.abs(tp.detach().numpy()), 1)) < 2e-2
+    rels = {}
+    for name, (o, s) in ref.OFF.items():
+        g_gpu = grads[o:o + s]
+        g_ref = P[name].grad.numpy().reshape(-1)
+        if name == "emb":  # only the rows of types that occur
+            used = np.unique(types)
+            g_gpu = g_gpu.reshape(64, 16)[used].ravel()
+            g_ref = g_ref.reshape(64, 16)[used].ravel()
+        if name == "b4":
+            g_gpu, g_ref = g_gpu[:1], g_ref[:1]
+        rels[name] = float(np.linalg.norm(g_gpu - g_ref) / max(np.linalg.norm(g_ref), 1e-12))
+    assert max(rels.values()) < 0.05, rels
+
+
+def test_training_reduces_loss_deterministically_and_checkpoints(built_library, tmp_path):
+    protein, ff = small_protein()
+    batch = synthetic_batch(BatchSpec("t", 8, 16, 64, 400, 800), protein, ff, 9)
+    params = []
+    for _ in range(2):
+        with GpuContext(0) as ctx:
+            ctx.upload_batch(batch)
+            ctx.surrogate_init(protein, ff, seed=1)
+            l1, _ = ctx.surrogate_train(1, batch_poses=512, lr=2e-3, seed=7)
+            l2, ms = ctx.surrogate_train(6, batch_poses=512, lr=2e-3, seed=8)
+            assert ms > 0 and l2 < l1
+            params.append(ctx.surrogate_params())
+            ctx.surrogate_score()
+            s1 = ctx.surrogate_download()
+            ctx.surrogate_save(str(tmp_path / "w.bin"))
+    assert np.array_equal(params[0], params[1])  # deterministic for a seed
+    with GpuContext(0) as ctx:
+        ctx.upload_batch(batch)
+        ctx.surrogate_init(protein, ff, seed=99)
+        ctx.surrogate_load(str(tmp_path / "w.bin"))
+        assert np.array_equal(ctx.surrogate_params(), params[0])
+        ctx.surrogate_score()
+        assert np.array_equal(ctx.surrogate_download(), s1)
+        with pytest.raises(BudeError):
+            ctx.surrogate_load(str(tmp_path / "missing.bin"))
+
+
+def exact_energies(ctx):
+    ctx.run_batch(launch_cfg(8, 128, 1, 64, 2))
+    return ctx.download_batch()
+
+
+def test_screen_invariants(built_library):
+    protein, ff = small_protein()
+    batch = synthetic_batch(BatchSpec("t", 12, 16, 64, 300, 2000), protein, ff, 11)
+    with GpuContext(0) as ctx:
+        ctx.upload_batch(batch)
+        exact = exact_energies(ctx)
+        ctx.surrogate_init(protein, ff, seed=2)
+        ctx.surrogate_train(4, batch_poses=1024, lr=2e-3, labels=exact, seed=3)
+        ctx.surrogate_score()
+        sur = ctx.surrogate_download()
+        st = ctx.screen(launch_cfg(8, 128, 1, 64, 2), top_frac=0.02, audit_frac=0.05, audit_tol=1e9, seed=5)
+        final, rescored, err = ctx.screen_download(batch.nligands)
+        off = batch.pose_offsets()
+        assert st["fallback_ligands"] == 0 and st["rescored_poses"] == rescored.sum()
+        for l in range(batch.nligands):
+            a, b = off[l], off[l + 1]
+            n = b - a
+            k = int(np.ceil(np.float32(0.02) * np.float32(n)))
+            picks = np.argsort(sur[a:b], kind="stable")[:k]
+            assert rescored[a:b][picks].all()
+            assert rescored[a:b].sum() >= k
+        # exact where rescored (same kernel, bit for bit), surrogate elsewhere
+        assert np.array_equal(final[rescored], exact[rescored])
+        assert np.array_equal(final[~rescored], sur[~rescored])
+        # an impossible tolerance sends every ligand to the exhaustive fallback
+        st = ctx.screen(launch_cfg(8, 128, 1, 64, 2), audit_tol=-1.0)
+        final, rescored, err = ctx.screen_download(batch.nligands)
+        assert st["fallback_ligands"] == batch.nligands and rescored.all()
+        assert np.array_equal(final, exact)
+
+
+def test_screen_ties_pick_first_poses(built_library):
+    # With every weight zero all surrogate scores tie: the picks are the first k poses of each
+    # ligand, in pose order.
+    protein, ff = small_protein()
+    batch = synthetic_batch(BatchSpec("t", 4, 16, 32, 100, 300), protein, ff, 12)
+    with GpuContext(0) as ctx:
+        ctx.upload_batch(batch)
+        ctx.surrogate_init(protein, ff, seed=2)
+        ctx.surrogate_params(np.zeros(ref.NPARAMS, np.float32))
+        ctx.screen(launch_cfg(8, 128), top_frac=0.1, audit_frac=0.0, audit_tol=1e9)
+        _, rescored, _ = ctx.screen_download(batch.nligands)
+        off = batch.pose_offsets()
+        for l in range(batch.nligands):
+            n = off[l + 1] - off[l]
+            k = int(np.ceil(np.float32(0.1) * np.float32(n)))
+            assert rescored[off[l]:off[l] + k].all() and not rescored[off[l] + k:off[l + 1]].any()
+
+
+def test_surrogate_errors(built_library):
+    protein, ff = small_protein()
+    with GpuContext(0) as ctx:
+        with pytest.raises(BudeError) as ei:
+            ctx.surrogate_init(protein, ff, extent=100.0, spacing=0.1)
+        assert ei.value.code == BUDE_ERR_ARG
+        big_ff = np.concatenate([ff, ff, ff])
+        with pytest.raises(BudeError):
+            ctx.surrogate_init(protein, big_ff)  # 102 types > 64
