@@ -49,9 +49,13 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["large", "small", "batch"], default="large",
+    ap.add_argument("--workload", choices=["large", "small", "batch", "surrogate", "screen"], default="large",
                     help="large: 4096 x 64 x 1M-pose deck (default); small: bm1-sized deck; batch: 256 ligands "
-                         "(12-96 atoms, 4096-65536 poses each) against the 2672-atom bm2 protein")
+                         "(12-96 atoms, 4096-65536 poses each) against the 2672-atom bm2 protein; surrogate: train on "
+                         "2M poses of 512 ligands (938-atom protein), score 64 held-out ligands x 65536 poses; screen: "
+                         "1024 ligands (16-80 atoms) x 16384 poses against the bm2 protein, surrogate-screened vs "
+                         "batched exhaustive exact")
+    ap.add_argument("--epochs", type=int, default=40, help="surrogate training epochs (surrogate/screen workloads)")
     ap.add_argument("--cfg", default="auto", help="auto, or ppwi,wgsize,split,tile[,unroll]")
     ap.add_argument("--nposes", type=int, default=0, help="use the first N poses of the deck (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
@@ -358,6 +362,133 @@ def run_batch(args, dist: Dist):
     return out
 
 
+def _recall_top(exact, score, off, frac=None, topn=None, budget=None, rescored=None):
+    """Mean over ligands of |exact top set in the candidate set| / |exact top set|: the candidate
+    set is the score's best `budget` (a count or fraction) poses, or the rescored poses."""
+    rec = []
+    for l in range(len(off) - 1):
+        a, b = off[l], off[l + 1]
+        n = b - a
+        k = topn if topn is not None else int(np.ceil(frac * n))
+        k = min(k, n)
+        if k == 0:
+            continue
+        truth = set(np.argsort(exact[a:b], kind="stable")[:k])
+        if rescored is not None:
+            cand = set(np.nonzero(rescored[a:b])[0])
+        else:
+            m = budget if isinstance(budget, int) else int(np.ceil(budget * n))
+            cand = set(np.argsort(score[a:b], kind="stable")[:m])
+        rec.append(len(truth & cand) / k)
+    return float(np.mean(rec)), float(np.min(rec))
+
+
+def run_surrogate(args, dist: Dist):
+    """Surrogate training on 2M exact-labelled poses and scoring of 64 held-out ligands x 65536 poses;
+    value = surrogate poses/s on the held-out set."""
+    from minibude_gb300 import BatchSpec, build, synthetic_batch
+    from minibude_gb300.model import GpuContext, launch_cfg
+    build.build_library()
+    d = synthetic_deck(SMALL, 0, 1)
+    protein, ff = d.protein, d.forcefield
+    train = synthetic_batch(BatchSpec("train-512x4096", 512, 16, 64, 4096, 4096), protein, ff, 100 + dist.rank)
+    held = synthetic_batch(BatchSpec("held-64x65536", 64, 16, 64, 65536, 65536), protein, ff, 200 + dist.rank)
+    ctx = GpuContext(dist.local_rank)
+    ctx.upload_batch(train)
+    ctx.surrogate_init(protein, ff, extent=11.0, spacing=0.4, seed=1)
+    loss, train_ms = ctx.surrogate_train(args.epochs, batch_poses=8192, lr=3e-3, seed=2)
+    ctx.upload_batch(held)
+    cfg, _ = ctx.autotune_batch()
+    ctx.run_batch(cfg)
+    exact_ms = ctx.run_batch(cfg)
+    exact = ctx.download_batch()
+    for _ in range(max(args.warmup, 1)):
+        ctx.surrogate_score()
+    launches0 = ctx.launch_count()
+    ms = [ctx.surrogate_score() for _ in range(args.steps)]
+    launches = ctx.launch_count() - launches0
+    sur = ctx.surrogate_download()
+    step = dist.max(float(np.mean(ms)))
+    off = held.pose_offsets()
+    r1 = _recall_top(exact, sur, off, frac=0.01, budget=0.01)
+    r2 = _recall_top(exact, sur, off, frac=0.01, budget=0.02)
+    rows = sum(len(l) * p.shape[1] for l, p in zip(held.ligands, held.poses))
+    out = {"metric": "surrogate poses/s", "value": round(dist.world * held.total_poses / (step * 1e-3), 1),
+           "unit": "poses/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16 (fp32 accumulate)", "data": "synthetic ligands/poses (seeded) against the 938-atom protein",
+           "config": {"workload": "surrogate-train-512x4096-held-64x65536", "train_poses": train.total_poses,
+                      "held_poses": held.total_poses, "epochs": args.epochs, "batch": 8192,
+                      "train_ms": round(train_ms, 1), "final_loss": round(loss, 3),
+                      "rmse": round(float(np.sqrt(np.mean((sur - exact) ** 2))), 3),
+                      "exact_std": round(float(exact.std()), 3),
+                      "recall_top1pct_in_surrogate_top1pct": {"mean": round(r1[0], 4), "min": round(r1[1], 4)},
+                      "recall_top1pct_in_surrogate_top2pct": {"mean": round(r2[0], 4), "min": round(r2[1], 4)},
+                      "exact_batched_ms": round(exact_ms, 3),
+                      "exact_batched_poses_per_s": round(held.total_poses / (exact_ms * 1e-3), 1),
+                      "mlp_rows_per_s": round(rows / (step * 1e-3), 1)},
+           "gpu_launches": launches}
+    ctx.close()
+    return out
+
+
+def run_screen(args, dist: Dist):
+    """Surrogate-screened scoring of 1024 ligands x 16384 poses against the bm2 protein, next to
+    batched exhaustive exact scoring; value = screened poses/s."""
+    from minibude_gb300 import BatchSpec, build, synthetic_batch
+    from minibude_gb300.model import GpuContext
+    build.build_library()
+    protein, ff = bm2_protein()
+    train = synthetic_batch(BatchSpec("train-512x4096", 512, 16, 80, 4096, 4096), protein, ff, 300 + dist.rank)
+    screen = synthetic_batch(BatchSpec("screen-1024x16384", 1024, 16, 80, 16384, 16384), protein, ff, 400 + dist.rank)
+    peaks = measured_peaks()
+    ctx = GpuContext(dist.local_rank)
+    ctx.upload_batch(train)
+    ctx.surrogate_init(protein, ff, extent=11.0, spacing=0.4, seed=1)
+    loss, train_ms = ctx.surrogate_train(args.epochs, batch_poses=8192, lr=3e-3, seed=2)
+    ctx.upload_batch(screen)
+    cfg, _ = ctx.autotune_batch()
+    # batched exhaustive exact scoring (the comparison, and the truth for recall)
+    ctx.run_batch(cfg)
+    ex_ms = [ctx.run_batch(cfg) for _ in range(max(2, args.steps // 2))]
+    exact = ctx.download_batch()
+    exhaustive_ms = float(np.mean(ex_ms))
+    for _ in range(max(args.warmup, 1)):
+        ctx.screen(cfg, top_frac=0.02, audit_frac=0.005, audit_tol=0.05, seed=7)
+    launches0 = ctx.launch_count()
+    with ClockSampler(dist.local_rank) as clocks:
+        dist.barrier()
+        stats = [ctx.screen(cfg, top_frac=0.02, audit_frac=0.005, audit_tol=0.05, seed=7) for _ in range(args.steps)]
+        dist.barrier()
+    launches = ctx.launch_count() - launches0
+    clk = clocks.summary(peaks.get("sm_max_mhz", 2070.0))
+    final, rescored, err = ctx.screen_download(screen.nligands)
+    step = dist.max(float(np.mean([st["total_ms"] for st in stats])))
+    off = screen.pose_offsets()
+    r100 = _recall_top(exact, final, off, topn=100, budget=100)
+    r1in = _recall_top(exact, final, off, frac=0.01, rescored=rescored)
+    last = stats[-1]
+    out = {"metric": "screened poses/s", "value": round(dist.world * screen.total_poses / (step * 1e-3), 1),
+           "unit": "poses/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16 surrogate + f32 exact",
+           "data": "synthetic ligands/poses (seeded) against the reference's bm2 protein",
+           "config": {"workload": "screen-1024x16384", "poses": screen.total_poses, "top_frac": 0.02,
+                      "audit_frac": 0.005, "audit_tol": 0.05, "epochs": args.epochs, "train_ms": round(train_ms, 1),
+                      "exhaustive_exact_ms": round(exhaustive_ms, 3),
+                      "exhaustive_exact_poses_per_s": round(screen.total_poses / (exhaustive_ms * 1e-3), 1),
+                      "speedup_vs_exhaustive": round(exhaustive_ms / step, 3),
+                      "recall_exact_top100": {"mean": round(r100[0], 4), "min": round(r100[1], 4)},
+                      "recall_exact_top1pct_rescored": {"mean": round(r1in[0], 4), "min": round(r1in[1], 4)},
+                      "surrogate_ms": round(last["surrogate_ms"], 3), "rescore_ms": round(last["rescore_ms"], 3),
+                      "fallback_ms": round(last["fallback_ms"], 3), "rescored_poses": int(last["rescored_poses"]),
+                      "fallback_ligands": int(last["fallback_ligands"]),
+                      "max_audit_error": round(float(last["max_audit_error"]), 4), "exact_launch": cfg.as_dict()},
+           "gpu_launches": launches, "clocks": clk}
+    ctx.close()
+    return out
+
+
 def run_reference(args, dist: Dist):
     """The reference arm: the reference's CPU implementation of the path on the host cores."""
     import oracle
@@ -410,6 +541,10 @@ def main():
             out = run_reference(args, dist)
         elif args.workload == "batch":
             out = run_batch(args, dist)
+        elif args.workload == "surrogate":
+            out = run_surrogate(args, dist)
+        elif args.workload == "screen":
+            out = run_screen(args, dist)
         else:
             out = run_ours(args, dist)
         if dist.rank == 0:

@@ -224,8 +224,8 @@ typedef struct bude_screen_stats {
 } bude_screen_stats;
 
 /* Surrogate scores every pose; per ligand the exact kernel rescores the top_frac best-scored poses
- * and an audit sample; a ligand whose audit error -- RMS(surrogate - exact) over its audit poses
- * / max(RMS deviation of those exact energies, 1) -- exceeds audit_tol is rescored exhaustively.
+ * and an audit sample; a ligand whose audit error -- 1 - Spearman rank correlation of surrogate and
+ * exact energies over its audit poses (at most 2048) -- exceeds audit_tol is rescored exhaustively.
  * Needs a trained (or loaded) surrogate and an uploaded batch. */
 int bude_screen_run(bude_gpu_ctx *ctx, const bude_screen_cfg *cfg, bude_screen_stats *stats);
 

@@ -8,8 +8,8 @@
 //      the pose index decides);
 //   3. the picked poses are compacted and rescored by the exact kernel (batch_kernel over the
 //      compact transforms);
-//   4. audit_kernel measures the surrogate's error on the audit sample: RMS(surrogate - exact) /
-//      max(RMS(exact - mean exact), 1); a ligand whose error exceeds `audit_tol` is rescored
+//   4. audit_kernel measures the surrogate's ordering error on the audit sample,
+//      1 - Spearman(surrogate, exact); a ligand whose error exceeds `audit_tol` is rescored
 //      exhaustively with the exact kernel;
 //   5. final energies: exact where rescored, the surrogate's elsewhere.
 // The exact kernel is the judge throughout: everything the screen reports as an energy of a
@@ -176,36 +176,58 @@ __global__ void __launch_bounds__(kSelThreads) compact_kernel(const long long *p
   }
 }
 
-// Per ligand: audit error = RMS(surrogate - exact) / max(RMS(exact - mean), 1) over its audit poses.
+// Per ligand: audit error = 1 - Spearman rank correlation between the surrogate and the exact
+// energies of its audit poses (at most kAuditMax of them, in pose order; average ranks for ties).
+// A pre-screen only has to order poses, so the audit measures the ordering.
+constexpr int kAuditMax = 2048;
+
 __global__ void __launch_bounds__(256) audit_kernel(const long long *comp_off, const int *counts,
                                                     const int *comp_pose, const float *comp_exact,
                                                     const float *scores, float *err) {
-  __shared__ double red[3][256];
+  __shared__ float sv[kAuditMax], ev[kAuditMax];
+  __shared__ double red[5][256];
   const int l = blockIdx.x;
   const long long a0 = comp_off[l] + counts[2 * l];
-  const int na = counts[2 * l + 1];
-  double se = 0, sx = 0, sxx = 0;
+  const int na = min(counts[2 * l + 1], kAuditMax);
   for (int i = threadIdx.x; i < na; i += blockDim.x) {
-    const double e = comp_exact[a0 + i], s = scores[comp_pose[a0 + i]];
-    se += (s - e) * (s - e);
-    sx += e;
-    sxx += e * e;
+    ev[i] = comp_exact[a0 + i];
+    sv[i] = scores[comp_pose[a0 + i]];
   }
-  red[0][threadIdx.x] = se;
-  red[1][threadIdx.x] = sx;
-  red[2][threadIdx.x] = sxx;
+  __syncthreads();
+  double sr = 0, er = 0, srr = 0, err2 = 0, ser = 0;
+  for (int i = threadIdx.x; i < na; i += blockDim.x) {
+    float rs = 0.f, re = 0.f;
+    for (int j = 0; j < na; ++j) {
+      rs += (sv[j] < sv[i]) ? 1.f : (sv[j] == sv[i] && j != i ? 0.5f : 0.f);
+      re += (ev[j] < ev[i]) ? 1.f : (ev[j] == ev[i] && j != i ? 0.5f : 0.f);
+    }
+    sr += rs;
+    er += re;
+    srr += (double)rs * rs;
+    err2 += (double)re * re;
+    ser += (double)rs * re;
+  }
+  red[0][threadIdx.x] = sr;
+  red[1][threadIdx.x] = er;
+  red[2][threadIdx.x] = srr;
+  red[3][threadIdx.x] = err2;
+  red[4][threadIdx.x] = ser;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
     if (threadIdx.x < o)
-      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+      for (int q = 0; q < 5; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    if (na == 0) {
-      err[l] = 0.f;
+    if (na < 3) {
+      err[l] = 0.f; // too few audit poses to judge: keep the picks
     } else {
-      const double mean = red[1][0] / na, var = fmax(0.0, red[2][0] / na - mean * mean);
-      err[l] = (float)(sqrt(red[0][0] / na) / fmax(sqrt(var), 1.0));
+      const double n = na;
+      const double cov = red[4][0] / n - (red[0][0] / n) * (red[1][0] / n);
+      const double vs = red[2][0] / n - (red[0][0] / n) * (red[0][0] / n);
+      const double ve = red[3][0] / n - (red[1][0] / n) * (red[1][0] / n);
+      const double rho = (vs > 0 && ve > 0) ? cov / sqrt(vs * ve) : 0.0;
+      err[l] = (float)(1.0 - rho);
     }
   }
 }
@@ -337,7 +359,10 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
     first.push_back(comp_off[l]);
     cnt.push_back(k);
   }
-  rc = run_items(c, s, cfg, range_items(c, lig, first, cnt, cfg.ppwi * cfg.wgsize), s.comp_xform.as<float4>(),
+  // Each ligand contributes only a few hundred picks: rescore them in 256-pose items so blocks are
+  // not mostly empty.
+  bude_launch_cfg small{4, 64, 1, 64, 2, 0};
+  rc = run_items(c, s, small, range_items(c, lig, first, cnt, small.ppwi * small.wgsize), s.comp_xform.as<float4>(),
                  s.comp_exact.as<float>());
   if (rc) return rc;
   cudaEventRecord(ev[2], c.stream);
