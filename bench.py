@@ -409,6 +409,12 @@ def run_surrogate(args, dist: Dist):
     launches = ctx.launch_count() - launches0
     sur = ctx.surrogate_download()
     step = dist.max(float(np.mean(ms)))
+    # the warp-level mma.sync scorer on the same network, for comparison
+    ctx.surrogate_set_scorer("mma_sync")
+    ctx.surrogate_score()
+    ms_sync = float(np.mean([ctx.surrogate_score() for _ in range(args.steps)]))
+    sur_sync = ctx.surrogate_download()
+    ctx.surrogate_set_scorer("tcgen05")
     off = held.pose_offsets()
     r1 = _recall_top(exact, sur, off, frac=0.01, budget=0.01)
     r2 = _recall_top(exact, sur, off, frac=0.01, budget=0.02)
@@ -426,7 +432,9 @@ def run_surrogate(args, dist: Dist):
                       "recall_top1pct_in_surrogate_top2pct": {"mean": round(r2[0], 4), "min": round(r2[1], 4)},
                       "exact_batched_ms": round(exact_ms, 3),
                       "exact_batched_poses_per_s": round(held.total_poses / (exact_ms * 1e-3), 1),
-                      "mlp_rows_per_s": round(rows / (step * 1e-3), 1)},
+                      "mlp_rows_per_s": round(rows / (step * 1e-3), 1), "scorer": "tcgen05",
+                      "mma_sync_scorer_poses_per_s": round(held.total_poses / (ms_sync * 1e-3), 1),
+                      "max_abs_diff_vs_mma_sync": round(float(np.max(np.abs(sur - sur_sync))), 4)},
            "gpu_launches": launches}
     ctx.close()
     return out

@@ -187,6 +187,14 @@ int bude_surrogate_train(bude_gpu_ctx *ctx, int32_t epochs, int32_t batch_poses,
 int bude_surrogate_score(bude_gpu_ctx *ctx, float *ms);
 int bude_surrogate_download(bude_gpu_ctx *ctx, float *scores, int64_t n);
 
+/* Which kernel scores poses (bude_surrogate_score and the screening pipeline):
+ * BUDE_SCORER_TCGEN05 (default) runs the three hidden layers as tcgen05 UMMAs with TMEM
+ * accumulators; BUDE_SCORER_MMA_SYNC runs them as warp-level mma.sync.  Both evaluate the same
+ * network with the same BF16 roundings; they differ only in FP32 summation order. */
+#define BUDE_SCORER_TCGEN05 0
+#define BUDE_SCORER_MMA_SYNC 1
+int bude_surrogate_set_scorer(bude_gpu_ctx *ctx, int32_t scorer);
+
 /* Loss gradient (no update) over the given batch poses with the given per-pose labels:
  * grads[BUDE_SURROGATE_NPARAMS] in the parameter layout, pred[n] the predicted energies. */
 int bude_surrogate_gradient(bude_gpu_ctx *ctx, const int32_t *poses, int32_t n, const float *labels, float *grads,

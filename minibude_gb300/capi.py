@@ -24,6 +24,9 @@ BUDE_ERR_STATE = -3
 BUDE_ERR_TIMEOUT = -4
 BUDE_ERR_TYPE = -5
 
+SCORER_TCGEN05 = 0
+SCORER_MMA_SYNC = 1
+
 STATUS_NAMES = {
     BUDE_OK: "BUDE_OK", BUDE_ERR_ARG: "BUDE_ERR_ARG", BUDE_ERR_CUDA: "BUDE_ERR_CUDA",
     BUDE_ERR_STATE: "BUDE_ERR_STATE", BUDE_ERR_TIMEOUT: "BUDE_ERR_TIMEOUT", BUDE_ERR_TYPE: "BUDE_ERR_TYPE",
@@ -99,6 +102,7 @@ SIGNATURES = [
                                             c_float_p]),
     ("bude_surrogate_score", ctypes.c_int, [_P, c_float_p]),
     ("bude_surrogate_download", ctypes.c_int, [_P, c_float_p, c_int64]),
+    ("bude_surrogate_set_scorer", ctypes.c_int, [_P, ctypes.c_int32]),
     ("bude_surrogate_gradient", ctypes.c_int, [_P, _P, c_int32, _P, c_float_p, c_float_p]),
     ("bude_surrogate_features", ctypes.c_int, [_P, _P, c_int32, c_float_p, _P]),
     ("bude_surrogate_params", ctypes.c_int, [_P, c_float_p, c_float_p, c_int64]),

@@ -57,6 +57,23 @@ __device__ __forceinline__ float silu(float z) {
   return z * s;
 }
 
+// The activation of the surrogate on a pair of pre-activations, as packed BF16:
+//   SiLU(z) = z * sigmoid(z) = hz + hz * tanh(hz),  hz = z / 2,
+// evaluated in BF16x2: hz rounded to BF16, one MUFU tanh for both values (tanh.approx.bf16x2,
+// sm_90+), one BF16x2 FMA.  Training and inference both use this function, so the trained weights
+// see exactly the activation that scores poses.  hz = bf16(z / 2) = bf16(z) / 2 exactly, so a
+// pre-activation saved as BF16 reproduces the same activation.
+// silu2_half takes the halved pre-activations z / 2 (hz before rounding) directly.
+__device__ __forceinline__ uint32_t silu2_half(float hz0, float hz1) {
+  const uint32_t hz = pack_bf16(hz0, hz1);
+  uint32_t t, h;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(hz));
+  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(h) : "r"(hz), "r"(t));
+  return h;
+}
+
+__device__ __forceinline__ uint32_t silu2(float z0, float z1) { return silu2_half(0.5f * z0, 0.5f * z1); }
+
 // d SiLU / dz = s * (1 + z * (1 - s)), s = sigmoid(z).
 __device__ __forceinline__ float silu_grad(float z) {
   const float s = fmaf(0.5f, tanh_approx(0.5f * z), 0.5f);

@@ -1,0 +1,236 @@
+// score_tc.cuh -- surrogate inference on the 5th-generation tensor cores (tcgen05 + TMEM).
+//
+// A block runs kTcGroups independent tile groups of 128 threads.  A group scores one item at a
+// time: up to 128 poses of one ligand, pose r = thread r = TMEM lane r of the group's 128 TMEM
+// columns.  For every ligand atom the group
+//   1. builds each pose's 32 features (surrogate_kernels.cuh: features_of; the field channels
+//      come from the texture unit) into its `act` tile, in the K-major core-matrix layout (tc.cuh);
+//   2. runs layers 1..3 as UMMAs issued by the group's first thread: D[128 x 128] = 1 * B_l^T
+//      (the bias) + act * (W_l / 2)^T over K = 32, 128, 128, FP32 accumulators in TMEM, completion
+//      signalled through the group's mbarrier;
+//   3. after each layer loads its row of D (= z / 2) from TMEM, applies the BF16x2 SiLU
+//      (mlp.cuh: silu2_half) and writes the BF16 row back into `act` as the next layer's input;
+//   4. runs the output layer as one more UMMA with N = 16: D[:, 0] + D[:, 1] = h3 . w4, with w4
+//      split into two BF16 parts (rows 0 and 1 of the B tile), and adds it to the pose's energy.
+// Halving W_l and b_l is exact in BF16/FP32, so D is exactly half of the FP32 sum the network
+// defines and the activation sees bf16(z / 2), as in training.  The bias enters as a K = 16 UMMA of
+// a tile of ones against b_l / 2 split into three BF16 parts (k = 0, 1, 2), so no FP32 add is left
+// in the epilogue.  The groups of a block share the weights in shared memory and interleave, so one
+// group's epilogue overlaps another's MMAs.  Every mbarrier wait is bounded; a wait that runs out
+// sets bit 0 of the error word, the group leaves at its next vote, and the block releases its TMEM.
+#pragma once
+#include <cstddef>
+
+#include "surrogate_kernels.cuh"
+#include "tc.cuh"
+
+namespace bude {
+
+constexpr int kTcGroups = 4;
+constexpr int kTcGroupThreads = 128; // warp w of a group reads TMEM lanes 32w .. 32w + 31
+constexpr int kTcThreads = kTcGroups * kTcGroupThreads;
+constexpr int kTcCols = 128;         // TMEM columns per group
+constexpr int kTcBiasK = 16;         // K of the bias UMMA (3 of 16 used)
+constexpr int kTcOutN = 16;          // N of the output UMMA (2 of 16 used)
+
+struct TcSmem {
+  alignas(128) unsigned char w1[kHid * kFeat * 2];          // W1 / 2: [128 out][32 in], K-major
+  alignas(128) unsigned char w2[kHid * kHid * 2];           // W2 / 2
+  alignas(128) unsigned char w3[kHid * kHid * 2];           // W3 / 2
+  alignas(128) unsigned char bias[3][kHid * kTcBiasK * 2];  // b_l / 2 in three BF16 parts at k = 0..2
+  alignas(128) unsigned char ones[kHid * kTcBiasK * 2];     // 1 at k = 0..2
+  alignas(128) unsigned char w4[kTcOutN * kHid * 2];        // w4 in two BF16 parts at n = 0, 1
+  alignas(128) unsigned char act[kTcGroups][kHid * kHid * 2]; // per group: the layer input tile
+  uint4 emb[kMaxTypes * 2];                                  // type embeddings (16 BF16 each)
+  alignas(8) uint64_t bar[kTcGroups];
+  uint32_t tmem;
+};
+
+static_assert(offsetof(TcSmem, w4) + sizeof(TcSmem::w4) - offsetof(TcSmem, bias) ==
+                  sizeof(TcSmem::bias) + sizeof(TcSmem::ones) + sizeof(TcSmem::w4),
+              "bias, ones and w4 tiles are contiguous (zeroed as one range)");
+static_assert(sizeof(TcSmem) <= 227 * 1024, "one block per SM fits the 227 KB shared-memory limit");
+static_assert(sizeof(TcSmem) > 114 * 1024, "shared memory keeps a second block (and its TMEM) off the SM");
+
+struct ScoreTcArgs {
+  ScoreArgs s;
+  unsigned int *err;
+};
+
+__device__ __forceinline__ void st_bf16(unsigned char *tile, uint32_t off, float v) {
+  *reinterpret_cast<__nv_bfloat16 *>(tile + off) = __float2bfloat16_rn(v);
+}
+
+// Copy a global [N][K] row-major BF16 matrix, halved (exact), into the K-major core-matrix layout.
+__device__ __forceinline__ void to_kmajor_half(unsigned char *dst, const __nv_bfloat16 *src, int n, int k) {
+  for (int i = threadIdx.x; i < n * k / 8; i += blockDim.x) {
+    const int row = i / (k / 8), k8 = i % (k / 8);
+    uint4 v = __ldg(reinterpret_cast<const uint4 *>(src + (long long)row * k + k8 * 8));
+    uint32_t *w = reinterpret_cast<uint32_t *>(&v);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float2 f = unpack_bf16(w[j]);
+      w[j] = pack_bf16(0.5f * f.x, 0.5f * f.y);
+    }
+    *reinterpret_cast<uint4 *>(dst + kmajor_offset(row, k8 * 8, k)) = v;
+  }
+}
+
+// The block's constant tiles: halved weights, bias and output tiles, the ones tile, embeddings.
+__device__ __forceinline__ void tc_setup(TcSmem &s, const MlpWeights &W) {
+  const int tid = threadIdx.x;
+  {
+    uint4 *z = reinterpret_cast<uint4 *>(s.bias);
+    const int n16 = (int)((sizeof s.bias + sizeof s.ones + sizeof s.w4) / 16);
+    for (int i = tid; i < n16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+  }
+  to_kmajor_half(s.w1, W.w1, kHid, kFeat);
+  to_kmajor_half(s.w2, W.w2, kHid, kHid);
+  to_kmajor_half(s.w3, W.w3, kHid, kHid);
+  for (int i = tid; i < kMaxTypes * 2; i += blockDim.x) s.emb[i] = __ldg(reinterpret_cast<const uint4 *>(W.emb) + i);
+  __syncthreads(); // zeroed tiles before their non-zero entries
+  for (int i = tid; i < 3 * kHid; i += blockDim.x) {
+    const int l = i / kHid, n = i % kHid;
+    const float *b = l == 0 ? W.b1 : (l == 1 ? W.b2 : W.b3);
+    const float v = 0.5f * __ldg(&b[n]);
+    const float hi = __bfloat162float(__float2bfloat16_rn(v));
+    const float mid = __bfloat162float(__float2bfloat16_rn(v - hi));
+    st_bf16(s.bias[l], kmajor_offset(n, 0, kTcBiasK), hi);
+    st_bf16(s.bias[l], kmajor_offset(n, 1, kTcBiasK), mid);
+    st_bf16(s.bias[l], kmajor_offset(n, 2, kTcBiasK), v - hi - mid);
+  }
+  for (int m = tid; m < kHid; m += blockDim.x)
+    for (int k = 0; k < 3; ++k) st_bf16(s.ones, kmajor_offset(m, k, kTcBiasK), 1.f);
+  for (int k = tid; k < kHid; k += blockDim.x) {
+    const float v = __ldg(&W.w4[k]);
+    const float hi = __bfloat162float(__float2bfloat16_rn(v));
+    st_bf16(s.w4, kmajor_offset(0, k, kHid), hi);
+    st_bf16(s.w4, kmajor_offset(1, k, kHid), v - hi);
+  }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) score_tc_kernel(const ScoreTcArgs A) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  TcSmem &s = *reinterpret_cast<TcSmem *>(smem_raw);
+  const ScoreArgs &a = A.s;
+  const int tid = threadIdx.x, g = tid / kTcGroupThreads, lt = tid % kTcGroupThreads;
+  const uint32_t bar_id = 1 + g; // named barrier of the group
+
+  tc_setup(s, a.W);
+  if (tid == 0) {
+    for (int q = 0; q < kTcGroups; ++q) mbar_init(&s.bar[q], 1);
+    mbar_fence_init();
+  }
+  if (tid < 32) tmem_alloc<kTcGroups * kTcCols>(&s.tmem);
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+
+  const uint32_t tmem = s.tmem + (uint32_t)(g * kTcCols);
+  const uint32_t lane_addr = tmem + ((uint32_t)((lt / 32) * 32) << 16);
+  unsigned char *act = s.act[g];
+  const uint32_t act_a = smem_u32(act), ones_a = smem_u32(s.ones);
+  const uint32_t idesc = umma_idesc_bf16(kHid, kHid), idesc_out = umma_idesc_bf16(kHid, kTcOutN);
+  const float b4 = __ldg(a.W.b4);
+  uint64_t *bar = &s.bar[g];
+  uint32_t phase = 0;
+  bool failed = false;
+
+  // Hidden layer: D = ones * bias^T + act * W^T over kdim, issued by the group's first thread.
+  auto hidden = [&](uint32_t w, uint32_t bias, int kdim) {
+    if (lt == 0) {
+      tc_fence_after();
+      const uint32_t sbo = (uint32_t)(kdim / 8) * 128u, bsbo = (kTcBiasK / 8) * 128u;
+      umma_bf16(tmem, umma_desc(ones_a, 128u, bsbo), umma_desc(bias, 128u, bsbo), idesc, 0u);
+      for (int kk = 0; kk < kdim / 16; ++kk)
+        umma_bf16(tmem, umma_desc(act_a + kk * 256u, 128u, sbo), umma_desc(w + kk * 256u, 128u, sbo), idesc, 1u);
+      umma_commit(bar);
+    }
+    if (!mbar_wait_bounded(bar, phase)) failed = true;
+    phase ^= 1u;
+    tc_fence_after();
+  };
+  // SiLU of the group's D rows into act (K = 128 layout), then the group barrier.
+  auto epilogue = [&]() {
+#pragma unroll 1
+    for (int c = 0; c < kHid / 32; ++c) {
+      uint32_t v[32];
+      tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
+      tmem_wait_ld();
+      uint32_t h[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) h[i] = silu2_half(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c * 32 + q * 8, kHid)) =
+            make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    named_sync(bar_id, kTcGroupThreads);
+  };
+
+  for (int item = blockIdx.x * kTcGroups + g; item < a.n_items; item += gridDim.x * kTcGroups) {
+    const int4 it = __ldg(&a.items[item]);
+    const float4 *xf = a.xform + (long long)(it.z + min(lt, it.w - 1)) * 3;
+    const float4 r0 = __ldg(xf), r1 = __ldg(xf + 1), r2 = __ldg(xf + 2);
+    float e = 0.f;
+    for (int il = 0; il < it.y; ++il) {
+      const float4 la = __ldg(&a.ligands[it.x + il]);
+      const int t = __float_as_int(la.w);
+      uint32_t f[kFeat / 2];
+      features_of(a.g, la, r0, r1, r2, s.emb[2 * t], s.emb[2 * t + 1], f);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, q * 8, kFeat)) =
+            make_uint4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+      fence_proxy_async();
+      tc_fence_before();
+      if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
+        failed = true;
+        break;
+      }
+      hidden(smem_u32(s.w1), smem_u32(s.bias[0]), kFeat);
+      epilogue();
+      hidden(smem_u32(s.w2), smem_u32(s.bias[1]), kHid);
+      epilogue();
+      hidden(smem_u32(s.w3), smem_u32(s.bias[2]), kHid);
+      epilogue();
+      // Output layer: h3 . w4 (two BF16 parts) in TMEM columns 0 and 1.
+      if (lt == 0) {
+        tc_fence_after();
+        const uint32_t sbo = (kHid / 8) * 128u;
+        const uint32_t w4a = smem_u32(s.w4);
+        for (int kk = 0; kk < kHid / 16; ++kk)
+          umma_bf16(tmem, umma_desc(act_a + kk * 256u, 128u, sbo), umma_desc(w4a + kk * 256u, 128u, sbo), idesc_out,
+                    kk > 0 ? 1u : 0u);
+        umma_commit(bar);
+      }
+      if (!mbar_wait_bounded(bar, phase)) failed = true;
+      phase ^= 1u;
+      tc_fence_after();
+      uint32_t y[2];
+      tmem_ld2(lane_addr, y);
+      tmem_wait_ld();
+      e += __uint_as_float(y[0]) + __uint_as_float(y[1]);
+      tc_fence_before(); // the next atom's barrier orders these TMEM reads before the next UMMA
+    }
+    // Group-uniform exit: every thread of the group leaves together.
+    if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
+      failed = true;
+      break;
+    }
+    if (lt < it.w) a.scores[it.z + lt] = e + (float)it.y * b4;
+  }
+  if (failed) {
+    atomicOr(A.err, 1u);
+    if (lt == 0) (void)mbar_wait_bounded(bar, phase ^ 1u); // an outstanding UMMA completes before TMEM goes
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (tid < 32) tmem_dealloc<kTcGroups * kTcCols>(s.tmem);
+}
+
+} // namespace bude

@@ -18,6 +18,7 @@
 
 #include "exact_kernel.cuh"
 #include "internal.h"
+#include "score_tc.cuh"
 #include "surrogate_kernels.cuh"
 
 namespace bude {
@@ -42,6 +43,8 @@ struct Surrogate {
   DevBuf params, adam_m, adam_v, grads;
   DevBuf emb_bf, w1_bf, w2_bf, w3_bf, w1t_bf, w2t_bf, w3t_bf;
   DevBuf grid, protein4;
+  cudaArray_t tex_arr[4] = {};
+  cudaTextureObject_t tex[4] = {};
   FieldGrid fg{};
   long long step = 0;
   // training scratch
@@ -52,6 +55,7 @@ struct Surrogate {
   DevBuf items, scores;
   int items_for = 0;
   int n_items = 0;
+  int scorer = BUDE_SCORER_TCGEN05;
 };
 
 static Surrogate &sur(Context &c) {
@@ -59,9 +63,19 @@ static Surrogate &sur(Context &c) {
   return *c.surrogate;
 }
 
+static void release_textures(Surrogate &s) {
+  for (int q = 0; q < 4; ++q) {
+    if (s.tex[q]) cudaDestroyTextureObject(s.tex[q]);
+    if (s.tex_arr[q]) cudaFreeArray(s.tex_arr[q]);
+    s.tex[q] = 0;
+    s.tex_arr[q] = nullptr;
+  }
+}
+
 void release_surrogate(Context &c) {
   if (!c.surrogate) return;
   Surrogate &s = *c.surrogate;
+  release_textures(s);
   DevBuf *all[] = {&s.params, &s.adam_m, &s.adam_v, &s.grads, &s.emb_bf, &s.w1_bf, &s.w2_bf, &s.w3_bf,
                    &s.w1t_bf, &s.w2t_bf, &s.w3t_bf, &s.grid, &s.protein4, &s.X, &s.row_type, &s.Z1,
                    &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3, &s.y, &s.dy, &s.pred, &s.loss, &s.part_w4,
@@ -109,12 +123,57 @@ static int set_smem_limits() {
   if (done) return BUDE_OK;
   cudaError_t e = cudaFuncSetAttribute(score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
   if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(score_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem));
+  if (e == cudaSuccess)
     e = cudaFuncSetAttribute(train_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(train_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(BwdSmem));
   if (e != cudaSuccess) return cuda_error(e, "surrogate shared-memory limits");
   done = true;
+  return BUDE_OK;
+}
+
+// The scaled FP32 grid (s.grid, n^3 voxels x 16) as four FP16 3-D textures with trilinear
+// filtering, clamped addressing and unnormalised coordinates.
+static int make_textures(Context &c, Surrogate &s, int n) {
+  release_textures(s);
+  const long long nvox = (long long)n * n * n;
+  DevBuf lin;
+  int rc = lin.reserve((size_t)nvox * 13 * sizeof(__half), "texture staging");
+  if (rc) return rc;
+  __half *t0 = lin.as<__half>(), *t1 = t0 + nvox * 4, *t2 = t1 + nvox * 4, *t3 = t2 + nvox * 4;
+  grid_pack_kernel<<<(unsigned)((nvox + 255) / 256), 256, 0, c.stream>>>(s.grid.as<float>(), nvox, t0, t1, t2, t3);
+  cudaError_t e = cudaStreamSynchronize(c.stream);
+  const __half *src[4] = {t0, t1, t2, t3};
+  for (int q = 0; q < 4 && e == cudaSuccess; ++q) {
+    const int ch = q < 3 ? 4 : 1;
+    cudaChannelFormatDesc fd = cudaCreateChannelDesc(16, ch > 1 ? 16 : 0, ch > 1 ? 16 : 0, ch > 1 ? 16 : 0,
+                                                     cudaChannelFormatKindFloat);
+    e = cudaMalloc3DArray(&s.tex_arr[q], &fd, make_cudaExtent(n, n, n));
+    if (e != cudaSuccess) break;
+    cudaMemcpy3DParms cp = {};
+    cp.srcPtr = make_cudaPitchedPtr(const_cast<__half *>(src[q]), (size_t)n * ch * sizeof(__half), n, n);
+    cp.dstArray = s.tex_arr[q];
+    cp.extent = make_cudaExtent(n, n, n);
+    cp.kind = cudaMemcpyDeviceToDevice;
+    e = cudaMemcpy3D(&cp);
+    if (e != cudaSuccess) break;
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = s.tex_arr[q];
+    cudaTextureDesc td = {};
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    e = cudaCreateTextureObject(&s.tex[q], &rd, &td, nullptr);
+  }
+  lin.release();
+  if (e != cudaSuccess) {
+    release_textures(s);
+    return cuda_error(e, "field grid textures");
+  }
   return BUDE_OK;
 }
 
@@ -218,10 +277,12 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
   dff.release();
   inv.release();
   if (e != cudaSuccess) return cuda_error(e, "field grid scaling");
-  s.fg.data = s.grid.as<float4>();
+  rc = make_textures(c, s, n);
+  s.grid.release();
+  if (rc) return rc;
+  for (int q = 0; q < 4; ++q) s.fg.tex[q] = s.tex[q];
   s.fg.ox = s.fg.oy = s.fg.oz = -extent;
   s.fg.inv_h = 1.f / spacing;
-  s.fg.nx = s.fg.ny = s.fg.nz = n;
   s.fg.xyz_scale = 0.1f;
   rc = publish(c, s);
   if (rc) return rc;
@@ -584,11 +645,23 @@ int surrogate_score_enqueue(Context &c, const float4 *xform_ready) {
   a.scores = s.scores.as<float>();
   a.n_items = s.n_items;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, score_kernel, kMlpThreads, sizeof(MlpSmem));
-  const int grid = std::min(s.n_items, std::max(1, per_sm) * std::max(c.num_sms, 1));
-  score_kernel<<<grid, kMlpThreads, sizeof(MlpSmem), c.stream>>>(a);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_error(e, "score_kernel launch");
+  cudaError_t e;
+  if (s.scorer == BUDE_SCORER_TCGEN05) {
+    ScoreTcArgs t;
+    t.s = a;
+    t.err = c.err.as<unsigned int>();
+    // One block per SM: a block holds all 512 TMEM columns of its SM.
+    const int grid = std::min((s.n_items + kTcGroups - 1) / kTcGroups, std::max(c.num_sms, 1));
+    score_tc_kernel<<<grid, kTcThreads, sizeof(TcSmem), c.stream>>>(t);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "score_tc_kernel launch");
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, score_kernel, kMlpThreads, sizeof(MlpSmem));
+    const int grid = std::min(s.n_items, std::max(1, per_sm) * std::max(c.num_sms, 1));
+    score_kernel<<<grid, kMlpThreads, sizeof(MlpSmem), c.stream>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "score_kernel launch");
+  }
   c.launches++;
   return BUDE_OK;
 }
@@ -674,6 +747,14 @@ int bude_surrogate_score(bude_gpu_ctx *ctx, float *ms) {
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_error(e, "surrogate scoring");
   if (ms) cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1);
+  return check_device_error(*ctx);
+}
+
+int bude_surrogate_set_scorer(bude_gpu_ctx *ctx, int32_t scorer) {
+  if (!ctx) return set_error(BUDE_ERR_ARG, "ctx is NULL");
+  if (scorer != BUDE_SCORER_TCGEN05 && scorer != BUDE_SCORER_MMA_SYNC)
+    return set_error(BUDE_ERR_ARG, "unknown surrogate scorer %d", (int)scorer);
+  sur(*ctx).scorer = scorer;
   return BUDE_OK;
 }
 

@@ -23,10 +23,12 @@
 //   c11      sum_{p: h_p<0} h_p * sat(1 - (r - (1.75+R_p))/1)
 //   c12      min_p (r - R_p), clamped to [-3, 8]
 // i.e. the distance-dependent shapes of the steric, charge and desolvation terms of the exact
-// kernel for a few probe atoms, each scaled to unit standard deviation over the grid.  They are
-// sampled trilinearly.
+// kernel for a few probe atoms, each scaled to unit standard deviation over the grid.  The scaled
+// grid is stored as four FP16 3-D textures (c0..c3, c4..c7, c8..c11, c12) and sampled with the
+// texture unit's trilinear filter, clamped at the grid's faces.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cstdint>
 
@@ -55,9 +57,8 @@ struct MlpWeights {
 };
 
 struct FieldGrid {
-  const float4 *data; // [nz][ny][nx][4] float4 = 16 channels, 13 used
-  float ox, oy, oz, inv_h;
-  int nx, ny, nz;
+  cudaTextureObject_t tex[4]; // FP16 3-D textures: c0..c3, c4..c7, c8..c11 (4 channels), c12 (1)
+  float ox, oy, oz, inv_h;    // grid origin and 1 / spacing
   float xyz_scale;
 };
 
@@ -124,48 +125,39 @@ __global__ void grid_scale_kernel(float *grid, long long nvox, const float *inv_
   grid[i] *= inv_scale[i % 16];
 }
 
-// Trilinear sample of the 13 channels at a position (clamped to the grid).
-__device__ __forceinline__ void sample_field(const FieldGrid &g, float x, float y, float z, float (&c)[kGridCh]) {
-  float u = (x - g.ox) * g.inv_h, v = (y - g.oy) * g.inv_h, w = (z - g.oz) * g.inv_h;
-  u = fminf(fmaxf(u, 0.f), g.nx - 1.001f);
-  v = fminf(fmaxf(v, 0.f), g.ny - 1.001f);
-  w = fminf(fmaxf(w, 0.f), g.nz - 1.001f);
-  const int i0 = (int)u, j0 = (int)v, k0 = (int)w;
-  const float fu = u - i0, fv = v - j0, fw = w - k0;
+// Split the scaled [voxels][16] FP32 grid into the texture layouts (FP16).
+__global__ void grid_pack_kernel(const float *grid, long long nvox, __half *t0, __half *t1, __half *t2, __half *t3) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvox) return;
+  const float *c = grid + v * 16;
+  __half *dst[3] = {t0, t1, t2};
 #pragma unroll
-  for (int k = 0; k < kGridCh; ++k) c[k] = 0.f;
+  for (int q = 0; q < 3; ++q)
 #pragma unroll
-  for (int corner = 0; corner < 8; ++corner) {
-    const int di = corner & 1, dj = (corner >> 1) & 1, dk = corner >> 2;
-    const float wt = (di ? fu : 1.f - fu) * (dj ? fv : 1.f - fv) * (dk ? fw : 1.f - fw);
-    const float4 *q = g.data + (((long long)(k0 + dk) * g.ny + (j0 + dj)) * g.nx + (i0 + di)) * 4;
-    const float4 a = __ldg(q), b = __ldg(q + 1), cc = __ldg(q + 2), d = __ldg(q + 3);
-    c[0] = fmaf(wt, a.x, c[0]);
-    c[1] = fmaf(wt, a.y, c[1]);
-    c[2] = fmaf(wt, a.z, c[2]);
-    c[3] = fmaf(wt, a.w, c[3]);
-    c[4] = fmaf(wt, b.x, c[4]);
-    c[5] = fmaf(wt, b.y, c[5]);
-    c[6] = fmaf(wt, b.z, c[6]);
-    c[7] = fmaf(wt, b.w, c[7]);
-    c[8] = fmaf(wt, cc.x, c[8]);
-    c[9] = fmaf(wt, cc.y, c[9]);
-    c[10] = fmaf(wt, cc.z, c[10]);
-    c[11] = fmaf(wt, cc.w, c[11]);
-    c[12] = fmaf(wt, d.x, c[12]);
-  }
+    for (int k = 0; k < 4; ++k) dst[q][v * 4 + k] = __float2half_rn(c[q * 4 + k]);
+  t3[v] = __float2half_rn(c[12]);
 }
 
-// Features of one (pose, ligand atom) as 16 packed BF16 pairs.
-__device__ __forceinline__ void atom_features(const MlpWeights &W, const FieldGrid &g, float4 la, const float4 *xf,
-                                              uint32_t (&f)[kFeat / 2]) {
-  const float4 r0 = __ldg(xf), r1 = __ldg(xf + 1), r2 = __ldg(xf + 2);
+// Trilinear sample of the 13 channels at a position.  Texel centres sit at integer + 0.5 in
+// unnormalised texture coordinates, so grid point i of axis u is at u = i + 0.5.
+__device__ __forceinline__ void sample_field(const FieldGrid &g, float x, float y, float z, float (&c)[kGridCh]) {
+  const float u = fmaf(x - g.ox, g.inv_h, 0.5f), v = fmaf(y - g.oy, g.inv_h, 0.5f), w = fmaf(z - g.oz, g.inv_h, 0.5f);
+  const float4 a = tex3D<float4>(g.tex[0], u, v, w);
+  const float4 b = tex3D<float4>(g.tex[1], u, v, w);
+  const float4 d = tex3D<float4>(g.tex[2], u, v, w);
+  c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w;
+  c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w;
+  c[8] = d.x; c[9] = d.y; c[10] = d.z; c[11] = d.w;
+  c[12] = tex3D<float>(g.tex[3], u, v, w);
+}
+
+// Features of one (pose, ligand atom) as 16 packed BF16 pairs, from the atom {x, y, z, type bits},
+// the pose's transform rows r0..r2 ({R row, t}) and the type's embedding e0, e1 (16 BF16).
+__device__ __forceinline__ void features_of(const FieldGrid &g, float4 la, float4 r0, float4 r1, float4 r2, uint4 e0,
+                                            uint4 e1, uint32_t (&f)[kFeat / 2]) {
   const float x = r0.w + la.x * r0.x + la.y * r0.y + la.z * r0.z;
   const float y = r1.w + la.x * r1.x + la.y * r1.y + la.z * r1.z;
   const float z = r2.w + la.x * r2.x + la.y * r2.y + la.z * r2.z;
-  const int t = __float_as_int(la.w);
-  const uint4 *e = reinterpret_cast<const uint4 *>(W.emb + t * kEmb);
-  const uint4 e0 = __ldg(e), e1 = __ldg(e + 1);
   f[0] = e0.x; f[1] = e0.y; f[2] = e0.z; f[3] = e0.w;
   f[4] = e1.x; f[5] = e1.y; f[6] = e1.z; f[7] = e1.w;
   float c[kGridCh];
@@ -178,6 +170,12 @@ __device__ __forceinline__ void atom_features(const MlpWeights &W, const FieldGr
   f[13] = pack_bf16(c[7], c[8]);
   f[14] = pack_bf16(c[9], c[10]);
   f[15] = pack_bf16(c[11], c[12]);
+}
+
+__device__ __forceinline__ void atom_features(const MlpWeights &W, const FieldGrid &g, float4 la, const float4 *xf,
+                                              uint32_t (&f)[kFeat / 2]) {
+  const uint4 *e = reinterpret_cast<const uint4 *>(W.emb + __float_as_int(la.w) * kEmb);
+  features_of(g, la, __ldg(xf), __ldg(xf + 1), __ldg(xf + 2), __ldg(e), __ldg(e + 1), f);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -243,8 +241,8 @@ __device__ __forceinline__ void act_to_frags(float (&acc)[16][4], const float *b
       z[j][0] = pack_bf16(z0, z1);
       z[j][1] = pack_bf16(z2, z3);
     }
-    const uint32_t lo = pack_bf16(silu(z0), silu(z1)); // row g
-    const uint32_t hi = pack_bf16(silu(z2), silu(z3)); // row g + 8
+    const uint32_t lo = silu2(z0, z1); // row g
+    const uint32_t hi = silu2(z2, z3); // row g + 8
     const int kk = j >> 1;
     if ((j & 1) == 0) {
       a[kk][0] = lo;
@@ -554,10 +552,11 @@ __global__ void __launch_bounds__(kMlpThreads) train_backward_kernel(BwdArgs a) 
       dz[j][1] = dy0 * s.w4[c0 + 1] * silu_grad(z[1]);
       dz[j][2] = dy1 * s.w4[c0] * silu_grad(z[2]);
       dz[j][3] = dy1 * s.w4[c0 + 1] * silu_grad(z[3]);
-      cs[j][0] = dy0 * silu(z[0]);
-      cs[j][1] = dy0 * silu(z[1]);
-      cs[j][2] = dy1 * silu(z[2]);
-      cs[j][3] = dy1 * silu(z[3]);
+      const float2 h0 = unpack_bf16(silu2(z[0], z[1])), h1 = unpack_bf16(silu2(z[2], z[3]));
+      cs[j][0] = dy0 * h0.x;
+      cs[j][1] = dy0 * h0.y;
+      cs[j][2] = dy1 * h1.x;
+      cs[j][3] = dy1 * h1.y;
     }
     colsum(cs);
     fold(acc_w4);
@@ -699,7 +698,7 @@ __global__ void __launch_bounds__(kMlpThreads) wgrad_kernel(WgradArgs a) {
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             const float2 f = unpack_bf16(w[q]);
-            w[q] = pack_bf16(silu(f.x), silu(f.y));
+            w[q] = silu2(f.x, f.y);
           }
         }
       }

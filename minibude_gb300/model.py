@@ -174,6 +174,13 @@ class GpuContext:
         check(self._lib.bude_surrogate_score(self.handle, ctypes.byref(ms)))
         return ms.value
 
+    def surrogate_set_scorer(self, scorer: str) -> None:
+        """Select the scoring kernel: "tcgen05" (default) or "mma_sync"."""
+        kinds = {"tcgen05": capi.SCORER_TCGEN05, "mma_sync": capi.SCORER_MMA_SYNC}
+        if scorer not in kinds:
+            raise ValueError(f"unknown scorer {scorer!r}; expected one of {sorted(kinds)}")
+        check(self._lib.bude_surrogate_set_scorer(self.handle, kinds[scorer]))
+
     def surrogate_download(self) -> np.ndarray:
         out = np.zeros(self.batch_poses, np.float32)
         check(self._lib.bude_surrogate_download(self.handle, fptr(out), self.batch_poses))

@@ -49,6 +49,22 @@ def test_forward_matches_torch(setup):
     assert np.max(np.abs(got[poses] - want) / scale) < 2e-2
 
 
+def test_tcgen05_and_mma_sync_scorers_agree(setup):
+    """The tensor-memory scorer and the warp-level one evaluate the same network; only their FP32
+    summation order differs, which may move a hidden activation by one BF16 step."""
+    ctx, batch = setup
+    out = {}
+    for kind in ("mma_sync", "tcgen05"):
+        ctx.surrogate_set_scorer(kind)
+        ctx.surrogate_score()
+        out[kind] = ctx.surrogate_download()
+    scale = np.maximum(np.abs(out["mma_sync"]), 1.0)
+    assert np.all(np.isfinite(out["tcgen05"]))
+    assert np.max(np.abs(out["tcgen05"] - out["mma_sync"]) / scale) < 5e-3
+    with pytest.raises(ValueError):
+        ctx.surrogate_set_scorer("wmma")
+
+
 def test_gradient_matches_torch_autograd(setup):
     ctx, batch = setup
     rng = np.random.default_rng(0)
