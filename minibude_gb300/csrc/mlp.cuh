@@ -1,5 +1,5 @@
 // mlp.cuh -- device helpers of the surrogate MLP: BF16 packing, warp-level BF16 tensor-core MMA
-// (mma.sync m16n8k16, FP32 accumulate), ldmatrix fragment loads and the SiLU activation.
+// (mma.sync m16n8k16, FP32 accumulate), ldmatrix fragment loads and the activation (hard-swish).
 //
 // Fragment layouts of mma.m16n8k16 (lane l, g = l / 4, t = l % 4):
 //   A 16x16 (row-major):  a0 = (g, 2t..2t+1)  a1 = (g+8, 2t..)  a2 = (g, 2t+8..)  a3 = (g+8, 2t+8..)
@@ -44,40 +44,24 @@ __device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const void *smem
                : "r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_row))));
 }
 
-// tanh on the MUFU unit (PTX tanh.approx.f32, sm_75+).
-__device__ __forceinline__ float tanh_approx(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
+// The activation of the surrogate: hard-swish, h(z) = z * sat(z / 6 + 1/2), evaluated in FP32 on
+// the FMA pipe (one FMA with saturation and one multiply per value; no MUFU operation) and rounded
+// to BF16 as the next layer's operand.  Training and inference both use act_pair, so the trained
+// weights see exactly the activation that scores poses.
+constexpr float kActSlope = 1.f / 6.f;
 
-// SiLU(z) = z * sigmoid(z), with sigmoid(z) = 0.5 + 0.5 * tanh(z / 2): one MUFU operation.
-__device__ __forceinline__ float silu(float z) {
-  const float s = fmaf(0.5f, tanh_approx(0.5f * z), 0.5f);
+__device__ __forceinline__ float act(float z) {
+  float s;
+  asm("fma.rn.sat.f32 %0, %1, %2, 0f3F000000;" : "=f"(s) : "f"(z), "f"(kActSlope));
   return z * s;
 }
 
-// The activation of the surrogate on a pair of pre-activations, as packed BF16:
-//   SiLU(z) = z * sigmoid(z) = hz + hz * tanh(hz),  hz = z / 2,
-// evaluated in BF16x2: hz rounded to BF16, one MUFU tanh for both values (tanh.approx.bf16x2,
-// sm_90+), one BF16x2 FMA.  Training and inference both use this function, so the trained weights
-// see exactly the activation that scores poses.  hz = bf16(z / 2) = bf16(z) / 2 exactly, so a
-// pre-activation saved as BF16 reproduces the same activation.
-// silu2_half takes the halved pre-activations z / 2 (hz before rounding) directly.
-__device__ __forceinline__ uint32_t silu2_half(float hz0, float hz1) {
-  const uint32_t hz = pack_bf16(hz0, hz1);
-  uint32_t t, h;
-  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(hz));
-  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(h) : "r"(hz), "r"(t));
-  return h;
-}
+// Two pre-activations -> packed BF16 activations (lo = z0, hi = z1).
+__device__ __forceinline__ uint32_t act_pair(float z0, float z1) { return pack_bf16(act(z0), act(z1)); }
 
-__device__ __forceinline__ uint32_t silu2(float z0, float z1) { return silu2_half(0.5f * z0, 0.5f * z1); }
-
-// d SiLU / dz = s * (1 + z * (1 - s)), s = sigmoid(z).
-__device__ __forceinline__ float silu_grad(float z) {
-  const float s = fmaf(0.5f, tanh_approx(0.5f * z), 0.5f);
-  return s * fmaf(z, 1.f - s, 1.f);
+// dh/dz: 0 below -3, 1 above 3, z / 3 + 1/2 between.
+__device__ __forceinline__ float act_grad(float z) {
+  return z <= -3.f ? 0.f : (z >= 3.f ? 1.f : fmaf(z, 2.f * kActSlope, 0.5f));
 }
 
 } // namespace bude

@@ -6,18 +6,17 @@
 //   1. builds each pose's 32 features (surrogate_kernels.cuh: features_of; the field channels
 //      come from the texture unit) into its `act` tile, in the K-major core-matrix layout (tc.cuh);
 //   2. runs layers 1..3 as UMMAs issued by the group's first thread: D[128 x 128] = 1 * B_l^T
-//      (the bias) + act * (W_l / 2)^T over K = 32, 128, 128, FP32 accumulators in TMEM, completion
+//      (the bias) + act * W_l^T over K = 32, 128, 128, FP32 accumulators in TMEM, completion
 //      signalled through the group's mbarrier;
-//   3. after each layer loads its row of D (= z / 2) from TMEM, applies the BF16x2 SiLU
-//      (mlp.cuh: silu2_half) and writes the BF16 row back into `act` as the next layer's input;
+//   3. after each layer loads its row of D (= z) from TMEM, applies the activation (mlp.cuh:
+//      act_pair, FMA pipe only) and writes the BF16 row back into `act` as the next layer's input;
 //   4. runs the output layer as one more UMMA with N = 16: D[:, 0] + D[:, 1] = h3 . w4, with w4
 //      split into two BF16 parts (rows 0 and 1 of the B tile), and adds it to the pose's energy.
-// Halving W_l and b_l is exact in BF16/FP32, so D is exactly half of the FP32 sum the network
-// defines and the activation sees bf16(z / 2), as in training.  The bias enters as a K = 16 UMMA of
-// a tile of ones against b_l / 2 split into three BF16 parts (k = 0, 1, 2), so no FP32 add is left
-// in the epilogue.  The groups of a block share the weights in shared memory and interleave, so one
-// group's epilogue overlaps another's MMAs.  Every mbarrier wait is bounded; a wait that runs out
-// sets bit 0 of the error word, the group leaves at its next vote, and the block releases its TMEM.
+// The bias enters as a K = 16 UMMA of a tile of ones against b_l split into three BF16 parts
+// (k = 0, 1, 2), so no FP32 add is left in the epilogue.  The groups of a block share the weights in
+// shared memory and interleave, so one group's epilogue overlaps another's MMAs.  Every mbarrier
+// wait is bounded; a wait that runs out sets bit 0 of the error word, the group leaves at its next
+// vote, and the block releases its TMEM.
 #pragma once
 #include <cstddef>
 
@@ -34,10 +33,10 @@ constexpr int kTcBiasK = 16;         // K of the bias UMMA (3 of 16 used)
 constexpr int kTcOutN = 16;          // N of the output UMMA (2 of 16 used)
 
 struct TcSmem {
-  alignas(128) unsigned char w1[kHid * kFeat * 2];          // W1 / 2: [128 out][32 in], K-major
-  alignas(128) unsigned char w2[kHid * kHid * 2];           // W2 / 2
-  alignas(128) unsigned char w3[kHid * kHid * 2];           // W3 / 2
-  alignas(128) unsigned char bias[3][kHid * kTcBiasK * 2];  // b_l / 2 in three BF16 parts at k = 0..2
+  alignas(128) unsigned char w1[kHid * kFeat * 2];          // W1: [128 out][32 in], K-major
+  alignas(128) unsigned char w2[kHid * kHid * 2];           // W2
+  alignas(128) unsigned char w3[kHid * kHid * 2];           // W3
+  alignas(128) unsigned char bias[3][kHid * kTcBiasK * 2];  // b_l in three BF16 parts at k = 0..2
   alignas(128) unsigned char ones[kHid * kTcBiasK * 2];     // 1 at k = 0..2
   alignas(128) unsigned char w4[kTcOutN * kHid * 2];        // w4 in two BF16 parts at n = 0, 1
   alignas(128) unsigned char act[kTcGroups][kHid * kHid * 2]; // per group: the layer input tile
@@ -61,38 +60,32 @@ __device__ __forceinline__ void st_bf16(unsigned char *tile, uint32_t off, float
   *reinterpret_cast<__nv_bfloat16 *>(tile + off) = __float2bfloat16_rn(v);
 }
 
-// Copy a global [N][K] row-major BF16 matrix, halved (exact), into the K-major core-matrix layout.
-__device__ __forceinline__ void to_kmajor_half(unsigned char *dst, const __nv_bfloat16 *src, int n, int k) {
+// Copy a global [N][K] row-major BF16 matrix into the K-major core-matrix layout.
+__device__ __forceinline__ void to_kmajor(unsigned char *dst, const __nv_bfloat16 *src, int n, int k) {
   for (int i = threadIdx.x; i < n * k / 8; i += blockDim.x) {
     const int row = i / (k / 8), k8 = i % (k / 8);
-    uint4 v = __ldg(reinterpret_cast<const uint4 *>(src + (long long)row * k + k8 * 8));
-    uint32_t *w = reinterpret_cast<uint32_t *>(&v);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const float2 f = unpack_bf16(w[j]);
-      w[j] = pack_bf16(0.5f * f.x, 0.5f * f.y);
-    }
-    *reinterpret_cast<uint4 *>(dst + kmajor_offset(row, k8 * 8, k)) = v;
+    *reinterpret_cast<uint4 *>(dst + kmajor_offset(row, k8 * 8, k)) =
+        __ldg(reinterpret_cast<const uint4 *>(src + (long long)row * k + k8 * 8));
   }
 }
 
-// The block's constant tiles: halved weights, bias and output tiles, the ones tile, embeddings.
-__device__ __forceinline__ void tc_setup(TcSmem &s, const MlpWeights &W) {
+// The block's constant tiles: weights, bias and output tiles, the ones tile, embeddings.
+template <class Smem> __device__ __forceinline__ void tc_setup(Smem &s, const MlpWeights &W) {
   const int tid = threadIdx.x;
   {
     uint4 *z = reinterpret_cast<uint4 *>(s.bias);
     const int n16 = (int)((sizeof s.bias + sizeof s.ones + sizeof s.w4) / 16);
     for (int i = tid; i < n16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
   }
-  to_kmajor_half(s.w1, W.w1, kHid, kFeat);
-  to_kmajor_half(s.w2, W.w2, kHid, kHid);
-  to_kmajor_half(s.w3, W.w3, kHid, kHid);
+  to_kmajor(s.w1, W.w1, kHid, kFeat);
+  to_kmajor(s.w2, W.w2, kHid, kHid);
+  to_kmajor(s.w3, W.w3, kHid, kHid);
   for (int i = tid; i < kMaxTypes * 2; i += blockDim.x) s.emb[i] = __ldg(reinterpret_cast<const uint4 *>(W.emb) + i);
   __syncthreads(); // zeroed tiles before their non-zero entries
   for (int i = tid; i < 3 * kHid; i += blockDim.x) {
     const int l = i / kHid, n = i % kHid;
     const float *b = l == 0 ? W.b1 : (l == 1 ? W.b2 : W.b3);
-    const float v = 0.5f * __ldg(&b[n]);
+    const float v = __ldg(&b[n]);
     const float hi = __bfloat162float(__float2bfloat16_rn(v));
     const float mid = __bfloat162float(__float2bfloat16_rn(v - hi));
     st_bf16(s.bias[l], kmajor_offset(n, 0, kTcBiasK), hi);
@@ -151,7 +144,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) score_tc_kernel(const ScoreTcAr
     phase ^= 1u;
     tc_fence_after();
   };
-  // SiLU of the group's D rows into act (K = 128 layout), then the group barrier.
+  // Activation of the group's D rows into act (K = 128 layout), then the group barrier.
   auto epilogue = [&]() {
 #pragma unroll 1
     for (int c = 0; c < kHid / 32; ++c) {
@@ -160,7 +153,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) score_tc_kernel(const ScoreTcAr
       tmem_wait_ld();
       uint32_t h[16];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) h[i] = silu2_half(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+      for (int i = 0; i < 16; ++i) h[i] = act_pair(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
 #pragma unroll
       for (int q = 0; q < 4; ++q)
         *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c * 32 + q * 8, kHid)) =

@@ -361,7 +361,7 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     reduce_parts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c.stream>>>(part, nparts, n, stride, dst);
   };
   // layer weight gradients
-  struct L { const __nv_bfloat16 *dz, *hin; int kin, silu; long long off; };
+  struct L { const __nv_bfloat16 *dz, *hin; int kin, act; long long off; };
   const L layers[3] = {{s.dZ3.as<__nv_bfloat16>(), s.Z2.as<__nv_bfloat16>(), kHid, 1, kOffW3},
                        {s.dZ2.as<__nv_bfloat16>(), s.Z1.as<__nv_bfloat16>(), kHid, 1, kOffW2},
                        {s.dZ1.as<__nv_bfloat16>(), s.X.as<__nv_bfloat16>(), kFeat, 0, kOffW1}};
@@ -369,7 +369,7 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     WgradArgs w;
     w.dZ = l.dz;
     w.Hin = l.hin;
-    w.apply_silu = l.silu;
+    w.apply_act = l.act;
     w.rows = (int)rows;
     w.chunk_rows = chunk;
     w.part = s.part_w.as<float>();

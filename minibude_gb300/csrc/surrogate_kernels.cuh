@@ -4,8 +4,8 @@
 // Model (all sizes fixed):
 //   features  x (32) = [type embedding (16) | transformed atom position * xyz_scale (3) |
 //                       13 protein-field channels sampled at the position]
-//   layers    z1 = W1 x + b1 (128), h1 = SiLU(z1); z2 = W2 h1 + b2, h2 = SiLU(z2);
-//             z3 = W3 h2 + b3, h3 = SiLU(z3); y = w4 . h3 + b4
+//   layers    z1 = W1 x + b1 (128), h1 = act(z1); z2 = W2 h1 + b2, h2 = act(z2);
+//             z3 = W3 h2 + b3, h3 = act(z3); y = w4 . h3 + b4,   act = hard-swish (mlp.cuh)
 //   pose      E_pose = sum over the ligand's atoms of y
 // Weights W1..W3 and the embedding are BF16 on the device for the tensor cores (FP32 masters and
 // FP32 Adam state are kept beside them); activations are rounded to BF16 between layers; every
@@ -228,7 +228,7 @@ __device__ __forceinline__ void layer_mma(float (&acc)[16][4], const uint32_t (&
   }
 }
 
-// bias + SiLU on a layer's accumulators and repack them as the next layer's A fragments;
+// bias + activation on a layer's accumulators and repack them as the next layer's A fragments;
 // z (optional) receives the pre-activations as BF16 pairs in accumulator layout.
 __device__ __forceinline__ void act_to_frags(float (&acc)[16][4], const float *bias, uint32_t (&a)[8][4],
                                              uint32_t (*z)[2]) {
@@ -241,8 +241,8 @@ __device__ __forceinline__ void act_to_frags(float (&acc)[16][4], const float *b
       z[j][0] = pack_bf16(z0, z1);
       z[j][1] = pack_bf16(z2, z3);
     }
-    const uint32_t lo = silu2(z0, z1); // row g
-    const uint32_t hi = silu2(z2, z3); // row g + 8
+    const uint32_t lo = act_pair(z0, z1); // row g
+    const uint32_t hi = act_pair(z2, z3); // row g + 8
     const int kk = j >> 1;
     if ((j & 1) == 0) {
       a[kk][0] = lo;
@@ -548,11 +548,11 @@ __global__ void __launch_bounds__(kMlpThreads) train_backward_kernel(BwdArgs a) 
       float z[4];
       zload(a.Z3, j, z);
       const int c0 = j * 8 + 2 * t;
-      dz[j][0] = dy0 * s.w4[c0] * silu_grad(z[0]);
-      dz[j][1] = dy0 * s.w4[c0 + 1] * silu_grad(z[1]);
-      dz[j][2] = dy1 * s.w4[c0] * silu_grad(z[2]);
-      dz[j][3] = dy1 * s.w4[c0 + 1] * silu_grad(z[3]);
-      const float2 h0 = unpack_bf16(silu2(z[0], z[1])), h1 = unpack_bf16(silu2(z[2], z[3]));
+      dz[j][0] = dy0 * s.w4[c0] * act_grad(z[0]);
+      dz[j][1] = dy0 * s.w4[c0 + 1] * act_grad(z[1]);
+      dz[j][2] = dy1 * s.w4[c0] * act_grad(z[2]);
+      dz[j][3] = dy1 * s.w4[c0 + 1] * act_grad(z[3]);
+      const float2 h0 = unpack_bf16(act_pair(z[0], z[1])), h1 = unpack_bf16(act_pair(z[2], z[3]));
       cs[j][0] = dy0 * h0.x;
       cs[j][1] = dy0 * h0.y;
       cs[j][2] = dy1 * h1.x;
@@ -593,7 +593,7 @@ __global__ void __launch_bounds__(kMlpThreads) train_backward_kernel(BwdArgs a) 
       fold(bacc);
     };
     to_frags(dz, a.dZ3, acc_b[2]);
-    // dh2 = dz3 W3 ; dz2 = dh2 * silu'(z2)
+    // dh2 = dz3 W3 ; dz2 = dh2 * act'(z2)
     float acc[16][4];
     layer_mma<8, kLdH>(acc, A, s.w3t);
 #pragma unroll
@@ -601,17 +601,17 @@ __global__ void __launch_bounds__(kMlpThreads) train_backward_kernel(BwdArgs a) 
       float z[4];
       zload(a.Z2, j, z);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * silu_grad(z[q]);
+      for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * act_grad(z[q]);
     }
     to_frags(dz, a.dZ2, acc_b[1]);
-    // dh1 = dz2 W2 ; dz1 = dh1 * silu'(z1)
+    // dh1 = dz2 W2 ; dz1 = dh1 * act'(z1)
     layer_mma<8, kLdH>(acc, A, s.w2t);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       float z[4];
       zload(a.Z1, j, z);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * silu_grad(z[q]);
+      for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * act_grad(z[q]);
     }
     to_frags(dz, a.dZ1, acc_b[0]);
     // dx (embedding columns 0..15) = dz1 W1: two n-tiles of W1^T rows 0..15.
@@ -654,11 +654,11 @@ __global__ void __launch_bounds__(kMlpThreads) train_backward_kernel(BwdArgs a) 
 }
 
 // Weight gradient partials of one layer: part[chunk] = dZ^T H over `chunk_rows` rows, with
-// H = SiLU(Zin) (or the features X for layer 1, kin = 32).  8 warps x 16 output rows.
+// H = act(Zin) (or the features X for layer 1, kin = 32).  8 warps x 16 output rows.
 struct WgradArgs {
   const __nv_bfloat16 *dZ;  // [rows][128]
-  const __nv_bfloat16 *Hin; // [rows][KIN]: pre-activations (apply SiLU) or features
-  int apply_silu;
+  const __nv_bfloat16 *Hin; // [rows][KIN]: pre-activations (apply act) or features
+  int apply_act;
   int rows;
   int chunk_rows; // multiple of 16
   float *part;    // [chunks][128][kin]
@@ -693,12 +693,12 @@ __global__ void __launch_bounds__(kMlpThreads) wgrad_kernel(WgradArgs a) {
       uint4 v = make_uint4(0, 0, 0, 0);
       if (r + rr < r_end) {
         v = *reinterpret_cast<const uint4 *>(a.Hin + (long long)(r + rr) * KIN + k8 * 8);
-        if (a.apply_silu) {
+        if (a.apply_act) {
           uint32_t *w = reinterpret_cast<uint32_t *>(&v);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             const float2 f = unpack_bf16(w[q]);
-            w[q] = silu2(f.x, f.y);
+            w[q] = act_pair(f.x, f.y);
           }
         }
       }

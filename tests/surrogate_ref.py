@@ -34,15 +34,10 @@ def bf(torch, t):
     return t + (t.to(torch.bfloat16).to(torch.float32) - t).detach()
 
 
-def silu(torch, z):
-    """The kernels' activation: hz = bf16(z / 2), t = bf16(tanh(hz)), h = bf16(hz + hz * t), i.e.
-    z * sigmoid(z) evaluated in BF16 (one MUFU tanh and one BF16 FMA per pair of values).  The
-    gradient is that of the exact FP32 SiLU, as the backward kernel computes it."""
-    exact = z * torch.sigmoid(z)
-    hz = (0.5 * z).to(torch.bfloat16).to(torch.float32)
-    t = torch.tanh(hz).to(torch.bfloat16).to(torch.float32)
-    emulated = (hz + hz * t).to(torch.bfloat16).to(torch.float32)
-    return exact + (emulated - exact).detach()
+def act(torch, z):
+    """The kernels' activation, hard-swish: z * sat(z / 6 + 1/2) in FP32 (rounded to BF16 by the
+    caller, as the kernels round it before the next layer)."""
+    return z * torch.clamp(z * (1.0 / 6.0) + 0.5, 0.0, 1.0)
 
 
 def row_outputs(torch, P, X, types):
@@ -50,9 +45,9 @@ def row_outputs(torch, P, X, types):
     rebuilt from P['emb'] so they carry gradients)."""
     x = torch.cat([bf(torch, P["emb"])[torch.as_tensor(types, dtype=torch.long)],
                    torch.as_tensor(X[:, 16:], dtype=torch.float32)], dim=1)
-    h1 = bf(torch, silu(torch, x @ bf(torch, P["W1"]).T + P["b1"]))
-    h2 = bf(torch, silu(torch, h1 @ bf(torch, P["W2"]).T + P["b2"]))
-    h3 = bf(torch, silu(torch, h2 @ bf(torch, P["W3"]).T + P["b3"]))
+    h1 = bf(torch, act(torch, x @ bf(torch, P["W1"]).T + P["b1"]))
+    h2 = bf(torch, act(torch, h1 @ bf(torch, P["W2"]).T + P["b2"]))
+    h3 = bf(torch, act(torch, h2 @ bf(torch, P["W3"]).T + P["b3"]))
     return h3 @ P["w4"] + P["b4"][0]
 
 
