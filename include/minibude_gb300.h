@@ -146,15 +146,18 @@ int bude_gpu_upload_batch(bude_gpu_ctx *ctx, const bude_atom *protein, int32_t n
                           const bude_atom *ligand_atoms, const int32_t *ligand_offsets, const float *poses,
                           int64_t pose_stride, const int64_t *pose_offsets);
 
-/* Launch shape for the batch (ppwi, wgsize, tile, unroll; split and cluster are not used): each
- * candidate is timed on a strided subset of the batch's work items.  Cached per batch. */
+/* Launch shape for the batch (ppwi, wgsize, tile, unroll, split; cluster is not used): each
+ * candidate is timed on a strided subset of the batch's work items, the best pose shape also with
+ * its protein cut into 2, 4 and 8 slices.  Cached per batch. */
 int bude_gpu_autotune_batch(bude_gpu_ctx *ctx, int32_t max_ms, bude_launch_cfg *best, float *best_ms);
 
 /* One evaluation of the whole batch, then a stream synchronise.  per_ligand = 0: one persistent
  * kernel over all (ligand, pose block) items, longest first, taken from an atomic work counter,
  * launched as a CUDA graph (counter reset + pose transforms + persistent kernel) captured on first
- * use of a launch shape.  per_ligand = 1: one plain exact-kernel launch per ligand, for
- * comparison.  *ms (optional) receives the CUDA-event time. */
+ * use of a launch shape.  With cfg->split > 1 (cluster ignored) every item is scored once per
+ * protein slice and a reduction kernel sums the slices in order; the energies then differ from
+ * split = 1 by FP32 summation order only.  per_ligand = 1: one plain exact-kernel launch per
+ * ligand, for comparison.  *ms (optional) receives the CUDA-event time. */
 int bude_gpu_run_batch(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, int32_t per_ligand, float *ms);
 
 /* Energies of the last batch evaluation, in concatenated pose order. */
@@ -220,7 +223,9 @@ typedef struct bude_screen_cfg {
   float audit_frac;   /* fraction of each ligand's poses rescored at random (audit sample) */
   float audit_tol;    /* audit error above which a ligand is rescored exhaustively */
   uint32_t seed;      /* audit sample */
-  bude_launch_cfg exact; /* launch shape of the exact rescoring (split/cluster unused) */
+  bude_launch_cfg exact; /* exact kernel of the exhaustive fallback (cluster unused); its split and
+                          * tile also cut the protein for the rescoring, so every exact energy the
+                          * screen reports equals bude_gpu_run_batch's with this shape, bit for bit */
 } bude_screen_cfg;
 
 typedef struct bude_screen_stats {

@@ -26,6 +26,7 @@ void release_batch(Context &c) {
   c.b_energies.release();
   c.b_items.release();
   c.b_counter.release();
+  c.b_partial.release();
   c.have_batch = false;
   c.items_ppb = 0;
   c.n_items = 0;
@@ -166,10 +167,26 @@ static int batch_blocks_per_sm(const bude_launch_cfg &cfg, int *per_sm) {
   return rc;
 }
 
+// Records per protein slice of a split evaluation: ceil(natpro_pad / split) in whole tiles.
+static int batch_slice(const Context &c, const bude_launch_cfg &cfg) {
+  const int per = (c.natpro_pad + cfg.split - 1) / cfg.split;
+  return (per + cfg.tile - 1) / cfg.tile * cfg.tile;
+}
+
+// The context's slice-sum buffer for a split evaluation of the whole batch.  Growing it moves the
+// buffer, so a captured graph that points at it is dropped first.
+static int reserve_batch_partial(Context &c, const bude_launch_cfg &cfg) {
+  if (cfg.split <= 1) return BUDE_OK;
+  const size_t bytes = (size_t)cfg.split * (size_t)std::max(c.batch_poses, 1LL) * sizeof(float);
+  if (bytes > c.b_partial.cap) drop_graph(c);
+  return c.b_partial.reserve(bytes, "batch slice sums");
+}
+
 // Enqueue the batch kernel over `items` (counter reset first): energies of the items' poses from
-// the transforms at `xform` into `energies`.
+// the transforms at `xform` into `energies` (through `partial` and a slice reduction when split).
 static int enqueue_items(Context &c, const bude_launch_cfg &cfg, int grid, const int4 *items, int n_items,
-                         const float4 *xform, float *energies) {
+                         const float4 *xform, float *energies, float *partial, long long npose_space) {
+  if (cfg.split > 1 && !partial) return set_error(BUDE_ERR_STATE, "split batch evaluation without a slice buffer");
   cudaError_t e = cudaMemsetAsync(c.b_counter.ptr, 0, sizeof(unsigned), c.stream);
   if (e != cudaSuccess) return cuda_error(e, "batch counter reset");
   BatchArgs a;
@@ -183,12 +200,22 @@ static int enqueue_items(Context &c, const bude_launch_cfg &cfg, int grid, const
   a.n_items = n_items;
   a.natpro_pad = c.natpro_pad;
   a.tile = cfg.tile;
+  a.split = std::max(cfg.split, 1);
+  a.slice = a.split > 1 ? batch_slice(c, cfg) : c.natpro_pad;
+  a.partial = partial;
+  a.npose_space = npose_space;
   const size_t smem = batch_smem(cfg);
 #define BUDE_LAUNCH(P, U) e = batch_launch_pu<P, U>(a, grid, cfg.wgsize, smem, c.stream)
   BUDE_BATCH_DISPATCH(cfg, BUDE_LAUNCH)
 #undef BUDE_LAUNCH
   if (e != cudaSuccess) return cuda_error(e, "batch_kernel launch");
   c.launches++;
+  if (a.split > 1 && n_items > 0) {
+    batch_reduce_kernel<<<(unsigned)n_items, 256, 0, c.stream>>>(items, partial, a.split, npose_space, energies);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "batch_reduce_kernel launch");
+    c.launches++;
+  }
   return BUDE_OK;
 }
 
@@ -201,7 +228,8 @@ static int enqueue_persistent(Context &c, const bude_launch_cfg &cfg, int grid, 
         c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>());
     c.launches++;
   }
-  return enqueue_items(c, cfg, grid, items, n_items, c.b_xform.as<float4>(), c.b_energies.as<float>());
+  return enqueue_items(c, cfg, grid, items, n_items, c.b_xform.as<float4>(), c.b_energies.as<float>(),
+                       c.b_partial.as<float>(), c.batch_poses);
 }
 
 static int persistent_grid(Context &c, const bude_launch_cfg &cfg, int *grid) {
@@ -215,11 +243,14 @@ static int persistent_grid(Context &c, const bude_launch_cfg &cfg, int *grid) {
 
 // The persistent evaluation as a CUDA graph, captured once per launch shape.
 static int ensure_graph(Context &c, const bude_launch_cfg &cfg) {
+  int rc = reserve_batch_partial(c, cfg); // may drop the graph
+  if (rc) return rc;
   const bool same = c.graph && c.graph_cfg.ppwi == cfg.ppwi && c.graph_cfg.wgsize == cfg.wgsize &&
-                    c.graph_cfg.tile == cfg.tile && c.graph_cfg.unroll == cfg.unroll;
+                    c.graph_cfg.tile == cfg.tile && c.graph_cfg.unroll == cfg.unroll &&
+                    c.graph_cfg.split == cfg.split;
   if (same) return BUDE_OK;
   drop_graph(c);
-  int rc = build_items(c, cfg.ppwi * cfg.wgsize);
+  rc = build_items(c, cfg.ppwi * cfg.wgsize);
   int grid = 0;
   if (!rc) rc = persistent_grid(c, cfg, &grid); // also sets the kernel's shared-memory limit
   if (rc) return rc;
@@ -245,17 +276,16 @@ static int ensure_graph(Context &c, const bude_launch_cfg &cfg) {
 }
 
 int batch_items_enqueue(Context &c, const bude_launch_cfg &cfg, const int4 *items, int n_items, const float4 *xform,
-                        float *energies) {
+                        float *energies, float *partial, long long npose_space) {
   int grid = 0;
   int rc = persistent_grid(c, cfg, &grid);
   if (rc) return rc;
-  return enqueue_items(c, cfg, grid, items, n_items, xform, energies);
+  return enqueue_items(c, cfg, grid, items, n_items, xform, energies, partial, npose_space);
 }
 
 int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand) {
   if (!c.have_batch) return set_error(BUDE_ERR_STATE, "no batch uploaded");
   bude_launch_cfg shape = cfg;
-  shape.split = 1;
   shape.cluster = 0;
   int rc = check_cfg(c, shape);
   if (rc) return rc;
@@ -264,7 +294,7 @@ int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand) {
     if (rc) return rc;
     cudaError_t e = cudaGraphLaunch(c.graph, c.stream);
     if (e != cudaSuccess) return cuda_error(e, "graph launch");
-    c.launches += c.batch_poses > 0 ? 2 : 1;
+    c.launches += (c.batch_poses > 0 ? 2 : 1) + (shape.split > 1 && c.n_items > 0 ? 1 : 0);
     return BUDE_OK;
   }
   // One plain exact-kernel launch per ligand, each with its own wave-model split (cluster
@@ -312,9 +342,22 @@ int autotune_batch(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  for (const Shape &sh : shapes) {
-    bude_launch_cfg cfg{sh.p, sh.w, 1, 64, sh.u, 0};
+  // Shapes at split 1 first; then the best of them with its protein cut into 2, 4 and 8 slices,
+  // which pays off when the batch is too small to keep every block slot busy to the end.
+  std::vector<bude_launch_cfg> cands;
+  for (const Shape &sh : shapes) cands.push_back(bude_launch_cfg{sh.p, sh.w, 1, 64, sh.u, 0});
+  const size_t n_shapes = cands.size();
+  for (size_t ci = 0; ci < cands.size(); ++ci) {
+    if (ci == n_shapes && best_t < 1e30f)
+      for (int sp : {2, 4, 8}) {
+        bude_launch_cfg v = best;
+        v.split = sp;
+        cands.push_back(v);
+      }
+    const bude_launch_cfg cfg = cands[ci];
     if (check_cfg(c, cfg)) continue;
+    rc = reserve_batch_partial(c, cfg);
+    if (rc) break;
     std::vector<int4> items;
     rc = build_items(c, cfg.ppwi * cfg.wgsize, &items);
     if (rc) break;
@@ -386,7 +429,6 @@ int bude_gpu_run_batch(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, int32_t pe
   if (ctx->have_batch && !per_ligand) {
     // Capture (or re-capture) before timing so the first timed launch is the graph itself.
     bude_launch_cfg shape = *cfg;
-    shape.split = 1;
     shape.cluster = 0;
     int rc = check_cfg(*ctx, shape);
     if (!rc) rc = ensure_graph(*ctx, shape);

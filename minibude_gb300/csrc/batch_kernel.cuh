@@ -8,6 +8,13 @@
 // (PosePairs::transform / tile, exact_kernel.cuh) over the whole protein, writes 0.5 * etot for
 // its poses and takes the next item.  The shared-memory ring and its mbarrier phases run on across
 // items (a global step counter), so no barrier is re-initialised.
+//
+// With split > 1 the protein is cut into `split` slices of `slice` records and every item is
+// scored once per slice (work unit v = item * split + slice, so the slices of an item follow each
+// other in the queue); each unit writes its slice sum to partial[slice][pose] and
+// batch_reduce_kernel folds the slices in slice order.  Many small items of uneven ligand size then
+// still spread evenly over the block slots.  The result is deterministic for a given split and
+// slice length.
 #pragma once
 #include "exact_kernel.cuh"
 
@@ -24,7 +31,26 @@ struct BatchArgs {
   int n_items;
   int natpro_pad;
   int tile;
+  int split;             // protein slices per item (1: energies written directly)
+  int slice;             // records per slice (a multiple of tile)
+  float *partial;        // split x npose_space slice sums when split > 1
+  long long npose_space; // pose index range of energies / partial rows
 };
+
+// Fold the slice sums of a split evaluation for the poses of each item (one block per item):
+// energies[p] = 0.5 * sum_s partial[s][p], summed in slice order (as slice_reduce_kernel does).
+// Poses outside the items keep their energies.
+static __global__ void __launch_bounds__(256) batch_reduce_kernel(const int4 *__restrict__ items,
+                                                            const float *__restrict__ partial, int split,
+                                                            long long npose_space, float *__restrict__ energies) {
+  const int4 it = items[blockIdx.x];
+  for (int i = threadIdx.x; i < it.w; i += blockDim.x) {
+    const long long p = (long long)it.z + i;
+    float acc = partial[p];
+    for (int s = 1; s < split; ++s) acc += partial[(long long)s * npose_space + p];
+    energies[p] = 0.5f * acc;
+  }
+}
 
 template <int P, int U>
 __global__ void __launch_bounds__(kMaxThreads) batch_kernel(const BatchArgs a) {
@@ -35,7 +61,7 @@ __global__ void __launch_bounds__(kMaxThreads) batch_kernel(const BatchArgs a) {
 
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
-  const int ntile = (a.natpro_pad + a.tile - 1) / a.tile;
+  const int n_units = a.n_items * a.split;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
@@ -48,11 +74,16 @@ __global__ void __launch_bounds__(kMaxThreads) batch_kernel(const BatchArgs a) {
   for (;;) {
     if (tid == 0) s_item = (int)atomicAdd(a.counter, 1u);
     __syncthreads();
-    const int item = s_item;
+    const int unit = s_item;
     __syncthreads(); // s_item is rewritten only after every thread has read it
-    if (item >= a.n_items) break;
+    if (unit >= n_units) break;
+    const int item = unit / a.split, sl = unit - item * a.split;
     const int4 it = __ldg(&a.items[item]);
     const float4 *lig = a.ligands + it.x;
+    // Protein records [a0, a1) of this unit's slice (empty past the end of the protein).
+    const int a0 = min(sl * a.slice, a.natpro_pad);
+    const int a1 = min(a.natpro_pad, a0 + a.slice);
+    const int ntile = (a1 - a0 + a.tile - 1) / a.tile;
     const int Q = it.y * ntile;
     const long long base = (long long)it.z + tid;
     const long long end = (long long)it.z + it.w;
@@ -61,8 +92,8 @@ __global__ void __launch_bounds__(kMaxThreads) batch_kernel(const BatchArgs a) {
       const int il = q / ntile;
       const int k = q - il * ntile;
       const int lt = __float_as_int(__ldg(&lig[il]).w);
-      const int first = k * a.tile;
-      const int cnt = min(a.tile, a.natpro_pad - first);
+      const int first = a0 + k * a.tile;
+      const int cnt = min(a.tile, a1 - first);
       const int s = (int)((qg + q) % kStages);
       const uint32_t bytes = (uint32_t)cnt * kRecF4 * sizeof(float4);
       mbar_arrive_expect_tx(&full[s], bytes);
@@ -87,7 +118,7 @@ __global__ void __launch_bounds__(kMaxThreads) batch_kernel(const BatchArgs a) {
         failed = true;
         continue;
       }
-      pp.template tile<U>(stages + (size_t)s * a.tile * kRecF4, min(a.tile, a.natpro_pad - k * a.tile));
+      pp.template tile<U>(stages + (size_t)s * a.tile * kRecF4, min(a.tile, a1 - (a0 + k * a.tile)));
     }
     const bool ok = !__syncthreads_or(failed || q < Q);
     if (!ok) {
@@ -99,10 +130,12 @@ __global__ void __launch_bounds__(kMaxThreads) batch_kernel(const BatchArgs a) {
       }
       return;
     }
+    float *out = a.split > 1 ? a.partial + (long long)sl * a.npose_space : a.energies;
+    const float scale = a.split > 1 ? 1.f : 0.5f;
 #pragma unroll
     for (int i = 0; i < P; ++i) {
       const long long pi = base + (long long)i * nthr;
-      if (pi < end) a.energies[pi] = 0.5f * pp.energy(i);
+      if (pi < end) out[pi] = scale * pp.energy(i);
     }
     qg += Q;
   }

@@ -42,6 +42,7 @@ struct Context {
   std::vector<long long> pose_off; // nligands + 1 pose offsets
   long long batch_poses = 0;
   DevBuf b_ligands, b_poses, b_xform, b_energies, b_items, b_counter;
+  DevBuf b_partial; // split x batch_poses slice sums of a split batch evaluation (graph-owned)
   int items_ppb = 0; // poses per item the device item list was built for
   int n_items = 0;
   cudaGraphExec_t graph = nullptr;
@@ -76,8 +77,11 @@ int choose_split(const Context &c, bude_launch_cfg &cfg);
 int choose_split_for(int num_sms, int natpro_pad, long long nposes, bude_launch_cfg &cfg);
 void release_batch(Context &c);
 int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand);
+// Batch kernel over `items` (energies of the items' poses from the transforms at `xform`).  With
+// cfg.split > 1 the slice sums go through `partial` (at least cfg.split * npose_space floats) and a
+// slice reduction over pose indices [0, npose_space).
 int batch_items_enqueue(Context &c, const bude_launch_cfg &cfg, const int4 *items, int n_items, const float4 *xform,
-                        float *energies);
+                        float *energies, float *partial, long long npose_space);
 void release_surrogate(Context &c);
 void release_screen(Context &c);
 int surrogate_score_enqueue(Context &c, const float4 *xform_ready);

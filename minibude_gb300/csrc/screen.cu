@@ -253,13 +253,14 @@ __global__ void fallback_copy_kernel(const long long *pose_off, const int *fallb
 
 struct ScreenState {
   DevBuf pose_off, flag, counts, comp_off, comp_pose, comp_xform, comp_exact, err, final_e, rescored, items, fb;
+  DevBuf partial; // slice sums of split exact evaluations
 };
 
 void release_screen(Context &c) {
   if (!c.screen) return;
   ScreenState &s = *c.screen;
   for (DevBuf *b : {&s.pose_off, &s.flag, &s.counts, &s.comp_off, &s.comp_pose, &s.comp_xform, &s.comp_exact,
-                    &s.err, &s.final_e, &s.rescored, &s.items, &s.fb})
+                    &s.err, &s.final_e, &s.rescored, &s.items, &s.fb, &s.partial})
     b->release();
   delete c.screen;
   c.screen = nullptr;
@@ -283,13 +284,17 @@ static std::vector<int4> range_items(const Context &c, const std::vector<int> &l
   return items;
 }
 
+// Exact energies of the items' poses (pose indices in [0, npose_space) of xform / energies).
 static int run_items(Context &c, ScreenState &s, const bude_launch_cfg &cfg, const std::vector<int4> &items,
-                     const float4 *xform, float *energies) {
+                     const float4 *xform, float *energies, long long npose_space) {
   if (items.empty()) return BUDE_OK;
   int rc = s.items.reserve(items.size() * sizeof(int4), "screen items");
+  if (!rc && cfg.split > 1)
+    rc = s.partial.reserve((size_t)cfg.split * (size_t)std::max(npose_space, 1LL) * sizeof(float), "screen slice sums");
   if (rc) return rc;
   cudaMemcpyAsync(s.items.ptr, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, c.stream);
-  rc = batch_items_enqueue(c, cfg, s.items.as<int4>(), (int)items.size(), xform, energies);
+  rc = batch_items_enqueue(c, cfg, s.items.as<int4>(), (int)items.size(), xform, energies, s.partial.as<float>(),
+                           npose_space);
   if (rc) return rc;
   // the host item vector must outlive the copy
   cudaError_t e = cudaStreamSynchronize(c.stream);
@@ -313,7 +318,6 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
   if (!rc) rc = s.rescored.reserve((size_t)std::max(np, 1LL), "rescored flags");
   if (rc) return rc;
   bude_launch_cfg cfg = sc.exact;
-  cfg.split = 1;
   cfg.cluster = 0;
   rc = check_cfg(c, cfg);
   if (rc) return rc;
@@ -360,10 +364,11 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
     cnt.push_back(k);
   }
   // Each ligand contributes only a few hundred picks: rescore them in 256-pose items so blocks are
-  // not mostly empty.
-  bude_launch_cfg small{4, 64, 1, 64, 2, 0};
+  // not mostly empty, with the fallback's protein slices (the pose shape does not change the
+  // arithmetic of a pose, the slices do).
+  const bude_launch_cfg small{4, 64, cfg.split, cfg.tile, 2, 0};
   rc = run_items(c, s, small, range_items(c, lig, first, cnt, small.ppwi * small.wgsize), s.comp_xform.as<float4>(),
-                 s.comp_exact.as<float>());
+                 s.comp_exact.as<float>(), ncomp);
   if (rc) return rc;
   cudaEventRecord(ev[2], c.stream);
   // 4. audit and fallback
@@ -384,7 +389,7 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
       fb_cnt.push_back((int)(c.pose_off[l + 1] - c.pose_off[l]));
     }
   rc = run_items(c, s, cfg, range_items(c, fb_lig, fb_first, fb_cnt, cfg.ppwi * cfg.wgsize), c.b_xform.as<float4>(),
-                 c.b_energies.as<float>());
+                 c.b_energies.as<float>(), np);
   if (rc) return rc;
   cudaEventRecord(ev[3], c.stream);
   // 5. final energies

@@ -77,6 +77,21 @@ def test_persistent_equals_per_ligand_unsplit(ctx, batch_and_refs):
     assert np.array_equal(persistent, np.concatenate(per_lig))
 
 
+@pytest.mark.parametrize("split,ppwi,wgsize", [(2, 8, 128), (5, 4, 64), (8, 16, 32), (64, 2, 64)])
+def test_split_batch_matches_oracle_and_is_deterministic(ctx, batch_and_refs, split, ppwi, wgsize):
+    # Protein slices per item (split 64 leaves some slices empty for the 2672-atom protein): parity
+    # with the oracle, and the same bits for every pose shape with the same split and tile.
+    b, (e32, e64) = batch_and_refs
+    ctx.upload_batch(b)
+    ctx.run_batch(launch_cfg(ppwi, wgsize, split, 64, 2, cluster=0))
+    got = ctx.download_batch()
+    assert_parity(got, e32, e64)
+    ctx.run_batch(launch_cfg(ppwi, wgsize, split, 64, 2, cluster=0))
+    assert np.array_equal(got, ctx.download_batch())
+    ctx.run_batch(launch_cfg(4, 128, split, 64, 1, cluster=0))
+    assert np.array_equal(got, ctx.download_batch())
+
+
 def test_per_ligand_mode_matches_oracle(ctx, batch_and_refs):
     b, (e32, e64) = batch_and_refs
     ctx.upload_batch(b)

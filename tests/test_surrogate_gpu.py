@@ -119,22 +119,24 @@ def test_training_reduces_loss_deterministically_and_checkpoints(built_library, 
             ctx.surrogate_load(str(tmp_path / "missing.bin"))
 
 
-def exact_energies(ctx):
-    ctx.run_batch(launch_cfg(8, 128, 1, 64, 2))
+def exact_energies(ctx, split=1):
+    ctx.run_batch(launch_cfg(8, 128, split, 64, 2, cluster=0))
     return ctx.download_batch()
 
 
-def test_screen_invariants(built_library):
+@pytest.mark.parametrize("split", [1, 4])
+def test_screen_invariants(built_library, split):
     protein, ff = small_protein()
     batch = synthetic_batch(BatchSpec("t", 12, 16, 64, 300, 2000), protein, ff, 11)
     with GpuContext(0) as ctx:
         ctx.upload_batch(batch)
-        exact = exact_energies(ctx)
+        exact = exact_energies(ctx, split)
         ctx.surrogate_init(protein, ff, seed=2)
         ctx.surrogate_train(4, batch_poses=1024, lr=2e-3, labels=exact, seed=3)
         ctx.surrogate_score()
         sur = ctx.surrogate_download()
-        st = ctx.screen(launch_cfg(8, 128, 1, 64, 2), top_frac=0.02, audit_frac=0.05, audit_tol=1e9, seed=5)
+        st = ctx.screen(launch_cfg(8, 128, split, 64, 2, cluster=0), top_frac=0.02, audit_frac=0.05, audit_tol=1e9,
+                        seed=5)
         final, rescored, err = ctx.screen_download(batch.nligands)
         off = batch.pose_offsets()
         assert st["fallback_ligands"] == 0 and st["rescored_poses"] == rescored.sum()
@@ -149,7 +151,7 @@ def test_screen_invariants(built_library):
         assert np.array_equal(final[rescored], exact[rescored])
         assert np.array_equal(final[~rescored], sur[~rescored])
         # an impossible tolerance sends every ligand to the exhaustive fallback
-        st = ctx.screen(launch_cfg(8, 128, 1, 64, 2), audit_tol=-1.0)
+        st = ctx.screen(launch_cfg(8, 128, split, 64, 2, cluster=0), audit_tol=-1.0)
         final, rescored, err = ctx.screen_download(batch.nligands)
         assert st["fallback_ligands"] == batch.nligands and rescored.all()
         assert np.array_equal(final, exact)
