@@ -56,6 +56,9 @@ def parse_args():
                          "1024 ligands (16-80 atoms) x 16384 poses against the bm2 protein, surrogate-screened vs "
                          "batched exhaustive exact")
     ap.add_argument("--epochs", type=int, default=40, help="surrogate training epochs (surrogate/screen workloads)")
+    ap.add_argument("--surrogate-ckpt", default=None,
+                    help="screen workload: load the trained surrogate from this file if it exists, else train and "
+                         "save it there")
     ap.add_argument("--cfg", default="auto", help="auto, or ppwi,wgsize,split,tile[,unroll]")
     ap.add_argument("--nposes", type=int, default=0, help="use the first N poses of the deck (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
@@ -161,9 +164,9 @@ def measured_peaks():
     return {}
 
 
-def traffic_per_launch(nposes: int):
-    """DRAM bytes per exact-kernel launch from the committed ncu summary (scaled to nposes)."""
-    path = os.path.join(ROOT, "profiles", "exact_kernel_traffic.txt")
+def traffic_per_launch(nposes: int, kernel: str = "exact_kernel"):
+    """DRAM bytes per launch of `kernel` from its committed ncu summary (scaled to nposes)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_traffic.txt")
     if not os.path.exists(path):
         return None
     vals = {}
@@ -383,6 +386,9 @@ def _recall_top(exact, score, off, frac=None, topn=None, budget=None, rescored=N
     return float(np.mean(rec)), float(np.min(rec))
 
 
+MLP_FLOP_PER_ROW = 2 * 128 * (32 + 128 + 128) + 2 * 128
+
+
 def run_surrogate(args, dist: Dist):
     """Surrogate training on 2M exact-labelled poses and scoring of 64 held-out ligands x 65536 poses;
     value = surrogate poses/s on the held-out set."""
@@ -419,6 +425,14 @@ def run_surrogate(args, dist: Dist):
     r1 = _recall_top(exact, sur, off, frac=0.01, budget=0.01)
     r2 = _recall_top(exact, sur, off, frac=0.01, budget=0.02)
     rows = sum(len(l) * p.shape[1] for l, p in zip(held.ligands, held.poses))
+    peaks = measured_peaks()
+    achieved = rows * MLP_FLOP_PER_ROW / (step * 1e-3) / 1e12
+    peak = float(peaks.get("bf16_tflops", 1900.8))
+    roof = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
+            "frac": round(achieved / peak, 4), "kernel": "score_tc_kernel",
+            "work": f"{MLP_FLOP_PER_ROW} FLOP per (pose, ligand atom) row: 2*128*(32+128+128) + 2*128",
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)" if "bf16_tflops" in peaks
+            else "fallback 1.9 PFLOP/s", "traffic": traffic_per_launch(held.total_poses, "score_tc_kernel")}
     out = {"metric": "surrogate poses/s", "value": round(dist.world * held.total_poses / (step * 1e-3), 1),
            "unit": "poses/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": round(step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -435,7 +449,7 @@ def run_surrogate(args, dist: Dist):
                       "mlp_rows_per_s": round(rows / (step * 1e-3), 1), "scorer": "tcgen05",
                       "mma_sync_scorer_poses_per_s": round(held.total_poses / (ms_sync * 1e-3), 1),
                       "max_abs_diff_vs_mma_sync": round(float(np.max(np.abs(sur - sur_sync))), 4)},
-           "gpu_launches": launches}
+           "gpu_launches": launches, "roofline": roof}
     ctx.close()
     return out
 
@@ -453,7 +467,13 @@ def run_screen(args, dist: Dist):
     ctx = GpuContext(dist.local_rank)
     ctx.upload_batch(train)
     ctx.surrogate_init(protein, ff, extent=11.0, spacing=0.4, seed=1)
-    loss, train_ms = ctx.surrogate_train(args.epochs, batch_poses=8192, lr=3e-3, seed=2)
+    if args.surrogate_ckpt and os.path.exists(args.surrogate_ckpt):
+        ctx.surrogate_load(args.surrogate_ckpt)
+        loss, train_ms = float("nan"), 0.0
+    else:
+        loss, train_ms = ctx.surrogate_train(args.epochs, batch_poses=8192, lr=3e-3, seed=2)
+        if args.surrogate_ckpt:
+            ctx.surrogate_save(args.surrogate_ckpt)
     ctx.upload_batch(screen)
     cfg, _ = ctx.autotune_batch()
     # batched exhaustive exact scoring (the comparison, and the truth for recall)
@@ -498,6 +518,16 @@ def run_screen(args, dist: Dist):
                       "max_audit_error": round(float(last["max_audit_error"]), 4), "exact_launch": cfg.as_dict(),
                       "screen_exact_launch": scfg.as_dict()},
            "gpu_launches": launches, "clocks": clk}
+    # dominant kernel: the surrogate scorer over every pose
+    rows = sum(len(l) * p.shape[1] for l, p in zip(screen.ligands, screen.poses))
+    sur_ms = float(np.mean([st["surrogate_ms"] for st in stats]))
+    achieved = rows * MLP_FLOP_PER_ROW / (sur_ms * 1e-3) / 1e12
+    peak = float(peaks.get("bf16_tflops", 1900.8))
+    out["roofline"] = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
+                       "frac": round(achieved / peak, 4), "kernel": "score_tc_kernel",
+                       "work": f"{MLP_FLOP_PER_ROW} FLOP per (pose, ligand atom) row",
+                       "share_of_step": round(sur_ms / step, 3),
+                       "traffic": traffic_per_launch(screen.total_poses, "score_tc_kernel")}
     ctx.close()
     return out
 
