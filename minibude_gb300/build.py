@@ -18,6 +18,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libbude_gb300.so")
 DRIVER_BIN = os.path.join(PKG, "bin", "gb300-bude")
+MAKEDECK_BIN = os.path.join(PKG, "bin", "gb300-makedeck")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -93,9 +94,24 @@ def build_driver(force: bool = False) -> str:
     return DRIVER_BIN
 
 
+def build_makedeck(force: bool = False) -> str:
+    """The deck generator binary (gb300-makedeck): makedeck's command line over the C-ABI."""
+    d = os.path.join(PKG, "makedeck")
+    srcs = [os.path.join(d, "main.cpp"), os.path.join(d, "deck_builder.cpp")]
+    deps = srcs + [os.path.join(d, "deck_builder.h"), LIB]
+    if not force and not _stale(MAKEDECK_BIN, deps):
+        return MAKEDECK_BIN
+    os.makedirs(os.path.dirname(MAKEDECK_BIN), exist_ok=True)
+    cxx = os.environ.get("CXX", "g++")
+    _run([cxx, "-std=c++17", "-O2", "-Wall", f"-I{INCLUDE}", f"-I{d}"] + srcs +
+         ["-o", MAKEDECK_BIN, f"-L{PKG}", "-lbude_gb300", f"-Wl,-rpath,{PKG}"])
+    return MAKEDECK_BIN
+
+
 def build_all(force: bool = False, verbose: bool = False) -> None:
     build_library(force=force, verbose=verbose)
     build_driver(force=force)
+    build_makedeck(force=force)
 
 
 if __name__ == "__main__":

@@ -275,6 +275,36 @@ class BatchDeck:
                          [np.ascontiguousarray(self.poses[l][:, :max_poses]) for l in ligands], self.name)
 
 
+FILE_CONFORMATIONS = "ligand_conformations.in"
+
+
+def read_conformations(deck_dir: str, natlig: int) -> list:
+    """The ligand conformations gb300-makedeck writes with --conformations (ligand_conformations.in:
+    natlig packed atom records per conformation, conformation after conformation); [] if absent."""
+    path = os.path.join(deck_dir, FILE_CONFORMATIONS)
+    if not os.path.isfile(path):
+        return []
+    recs = _read_n_struct(path, ATOM_DTYPE)
+    if natlig <= 0 or recs.size % natlig:
+        raise ValueError(f"{path}: {recs.size} atom records is not a whole number of {natlig}-atom conformations")
+    return [np.ascontiguousarray(recs[i:i + natlig]) for i in range(0, recs.size, natlig)]
+
+
+def conformation_batch(deck: Deck, conformations: list, include_deck_ligand: bool = True) -> "BatchDeck":
+    """Every conformation of the deck's ligand against every pose of the deck, as a batch: ligand l
+    of the batch is conformation l (the deck's own ligand first when include_deck_ligand), each with
+    the deck's poses, so one batched launch scores conformations x poses.  The reference's deck
+    generator parses the @<BUDE>CONF conformations of a mol2 and drops them
+    (makedeck/input-utils.cpp:185-200)."""
+    ligs = ([deck.ligand] if include_deck_ligand else []) + list(conformations)
+    for c in ligs:
+        if len(c) != len(deck.ligand) or not np.array_equal(c["type"], deck.ligand["type"]):
+            raise ValueError("a conformation must have the ligand's atoms (same count and types)")
+    poses = np.ascontiguousarray(deck.poses, np.float32)
+    return BatchDeck(deck.protein, deck.forcefield, [np.ascontiguousarray(c, ATOM_DTYPE) for c in ligs],
+                     [poses] * len(ligs), f"{deck.path} conformations")
+
+
 @dataclasses.dataclass(frozen=True)
 class BatchSpec:
     """Shape of a synthetic batch: ligand atom counts uniform in [atoms_lo, atoms_hi], pose counts
