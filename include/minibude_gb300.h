@@ -126,6 +126,17 @@ int bude_gpu_download(bude_gpu_ctx *ctx, float *energies, int64_t nposes);
 int bude_gpu_score_host(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, const bude_atom *ligand, int32_t natlig,
                         const float *poses, int64_t pose_stride, int64_t nposes, float *energies);
 
+/* Evaluate poses that stay in host memory, `chunk` poses at a time, against the uploaded deck's
+ * protein and ligand: chunk i+1's poses are copied in and chunk i-1's energies copied out while
+ * chunk i is evaluated (two copy streams beside the context's stream).  Replaces the whole-deck
+ * H2D copy of src/cuda/fasten.hpp:256-270 for decks too large to stage at once or produced on the
+ * host.  poses: six fields at poses + k*pose_stride (poses.in layout); energies: nposes floats.
+ * Pinned host buffers (bude_host_alloc) let the copies overlap.  The energies equal those of
+ * bude_gpu_run with the same cfg over all poses, bit for bit, for any chunk.  *ms (optional):
+ * CUDA-event time of the whole call.  No counterpart in the reference. */
+int bude_gpu_score_stream(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, const float *poses, int64_t pose_stride,
+                          int64_t nposes, int64_t chunk, float *energies, float *ms);
+
 /* The whole of CudaBude<PPWI>::fasten (src/cuda/fasten.hpp:250-305) in one call: create a context
  * on `device`, upload, run `iterations` times, download, destroy.  kernel_ms (optional) receives
  * `iterations` per-iteration times, context_ms (optional) the upload time. */

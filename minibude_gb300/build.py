@@ -24,7 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
 # Translation units of libbude_gb300.so; each compiles in parallel.
-CU_SOURCES = ["bude_gb300.cu", "autotune.cu", "batch.cu", "surrogate.cu", "screen.cu", "noalloc.cu", "arch_probe.cu"]
+CU_SOURCES = ["bude_gb300.cu", "autotune.cu", "batch.cu", "surrogate.cu", "screen.cu", "noalloc.cu", "stream.cu",
+              "arch_probe.cu"]
 
 
 def nvcc() -> str:

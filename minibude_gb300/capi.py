@@ -90,6 +90,8 @@ SIGNATURES = [
     ("bude_gpu_download", ctypes.c_int, [_P, c_float_p, c_int64]),
     ("bude_gpu_score_host", ctypes.c_int, [_P, ctypes.POINTER(BudeLaunchCfg), _P, c_int32, _P, c_int64, c_int64,
                                            c_float_p]),
+    ("bude_gpu_score_stream", ctypes.c_int, [_P, ctypes.POINTER(BudeLaunchCfg), _P, c_int64, c_int64, c_int64,
+                                             c_float_p, c_float_p]),
     ("bude_gpu_fasten", ctypes.c_int, [ctypes.c_int, c_int32, c_int32, _P, c_int32, _P, c_int32, _P, c_int32, _P,
                                        c_int64, c_int64, c_int32, c_float_p, c_float_p, c_float_p]),
     ("bude_gpu_upload_batch", ctypes.c_int, [_P, _P, c_int32, _P, c_int32, c_int32, _P, _P, _P, c_int64, _P]),

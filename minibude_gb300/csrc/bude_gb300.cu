@@ -375,6 +375,7 @@ void destroy_context(Context *c) {
   release_batch(*c);
   release_surrogate(*c);
   release_screen(*c);
+  release_streamer(*c);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);

@@ -12,6 +12,7 @@ namespace bude {
 
 struct Surrogate;
 struct ScreenState;
+struct StreamState;
 
 // A growable device allocation.
 struct DevBuf {
@@ -52,6 +53,7 @@ struct Context {
   float batch_tuned_ms = 0.f;
   Surrogate *surrogate = nullptr; // learned pre-screen (surrogate.cu)
   ScreenState *screen = nullptr;  // last screening run (screen.cu)
+  StreamState *streamer = nullptr; // chunked evaluation of host-resident poses (stream.cu)
   // autotuner cache: the deck shape it was tuned for and the pick
   long long tuned_key[3] = {-1, -1, -1};
   bude_launch_cfg tuned{};
@@ -83,6 +85,7 @@ int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand);
 int batch_items_enqueue(Context &c, const bude_launch_cfg &cfg, const int4 *items, int n_items, const float4 *xform,
                         float *energies, float *partial, long long npose_space);
 void release_surrogate(Context &c);
+void release_streamer(Context &c);
 void release_screen(Context &c);
 int surrogate_score_enqueue(Context &c, const float4 *xform_ready);
 float *surrogate_scores(Context &c);

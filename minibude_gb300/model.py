@@ -127,6 +127,20 @@ class GpuContext:
         self.nposes = poses.shape[1]
         return energies
 
+    def score_stream(self, cfg: BudeLaunchCfg, poses: np.ndarray, energies: np.ndarray, chunk: int = 65536) -> float:
+        """Evaluate host-resident poses (six fields, [6][n] or any array with a row stride) against
+        the uploaded deck's protein and ligand, `chunk` poses at a time with copies overlapped;
+        returns the CUDA-event time in ms.  Energies land in `energies` (n floats)."""
+        if poses.ndim != 2 or poses.shape[0] != 6 or poses.dtype != np.float32 or poses.strides[1] != 4:
+            raise ValueError("poses must be a float32 [6][n] array with contiguous rows")
+        n, stride = poses.shape[1], poses.strides[0] // 4
+        if energies.dtype != np.float32 or energies.size < n or not energies.flags.c_contiguous:
+            raise ValueError("energies must be a contiguous float32 array of at least n values")
+        ms = ctypes.c_float()
+        check(self._lib.bude_gpu_score_stream(self.handle, ctypes.byref(cfg), ctypes.c_void_p(poses.ctypes.data),
+                                              stride, n, chunk, fptr(energies), ctypes.byref(ms)))
+        return ms.value
+
     # -- batches of ligands -------------------------------------------------------------------
     def upload_batch(self, batch) -> None:
         protein, ff = _atoms(batch.protein), _ff(batch.forcefield)

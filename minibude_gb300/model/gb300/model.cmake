@@ -23,6 +23,7 @@ macro(setup)
             ${GB300_ROOT}/minibude_gb300/csrc/surrogate.cu
             ${GB300_ROOT}/minibude_gb300/csrc/screen.cu
             ${GB300_ROOT}/minibude_gb300/csrc/noalloc.cu
+            ${GB300_ROOT}/minibude_gb300/csrc/stream.cu
             ${GB300_ROOT}/minibude_gb300/csrc/arch_probe.cu)
     target_include_directories(bude_gb300 PUBLIC ${GB300_ROOT}/include)
     target_compile_options(bude_gb300 PRIVATE
