@@ -237,8 +237,14 @@ typedef struct bude_screen_cfg {
   bude_launch_cfg exact; /* exact kernel of the exhaustive fallback (cluster unused); its split and
                           * tile also cut the protein for the rescoring, so every exact energy the
                           * screen reports equals bude_gpu_run_batch's with this shape, bit for bit */
+  int32_t chunks;     /* ligand chunks (0 or 1: none): with more, the exact rescoring of chunk j
+                       * runs beside the surrogate of chunk j+1 (slower on the 1,024-ligand
+                       * screen: the rescoring blocks slow the surrogate more than they hide) */
 } bude_screen_cfg;
 
+/* total_ms: the whole call; surrogate_ms: pose transforms and surrogate scoring (until the last
+ * chunk's scorer has finished); rescore_ms: selection, compaction and exact rescoring after that;
+ * fallback_ms: the audit and the exhaustive fallback. */
 typedef struct bude_screen_stats {
   float total_ms, surrogate_ms, rescore_ms, fallback_ms;
   int64_t rescored_poses;  /* picks + audit */
@@ -247,8 +253,9 @@ typedef struct bude_screen_stats {
   float max_audit_error;
 } bude_screen_stats;
 
-/* Surrogate scores every pose; per ligand the exact kernel rescores the top_frac best-scored poses
- * and an audit sample; a ligand whose audit error -- 1 - Spearman rank correlation of surrogate and
+/* Surrogate scores every pose; per ligand the exact kernel rescores the ceil(top_frac * n)
+ * best-scored poses and an audit sample of ceil(audit_frac * n) of the others (uniform, seeded);
+ * a ligand whose audit error -- 1 - Spearman rank correlation of surrogate and
  * exact energies over its audit poses (at most 2048) -- exceeds audit_tol is rescored exhaustively.
  * Needs a trained (or loaded) surrogate and an uploaded batch. */
 int bude_screen_run(bude_gpu_ctx *ctx, const bude_screen_cfg *cfg, bude_screen_stats *stats);

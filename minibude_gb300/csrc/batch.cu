@@ -185,9 +185,11 @@ static int reserve_batch_partial(Context &c, const bude_launch_cfg &cfg) {
 // Enqueue the batch kernel over `items` (counter reset first): energies of the items' poses from
 // the transforms at `xform` into `energies` (through `partial` and a slice reduction when split).
 static int enqueue_items(Context &c, const bude_launch_cfg &cfg, int grid, const int4 *items, int n_items,
-                         const float4 *xform, float *energies, float *partial, long long npose_space) {
+                         const float4 *xform, float *energies, float *partial, long long npose_space,
+                         cudaStream_t st = nullptr) {
+  if (!st) st = c.stream;
   if (cfg.split > 1 && !partial) return set_error(BUDE_ERR_STATE, "split batch evaluation without a slice buffer");
-  cudaError_t e = cudaMemsetAsync(c.b_counter.ptr, 0, sizeof(unsigned), c.stream);
+  cudaError_t e = cudaMemsetAsync(c.b_counter.ptr, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return cuda_error(e, "batch counter reset");
   BatchArgs a;
   a.ligands = c.b_ligands.as<float4>();
@@ -205,13 +207,13 @@ static int enqueue_items(Context &c, const bude_launch_cfg &cfg, int grid, const
   a.partial = partial;
   a.npose_space = npose_space;
   const size_t smem = batch_smem(cfg);
-#define BUDE_LAUNCH(P, U) e = batch_launch_pu<P, U>(a, grid, cfg.wgsize, smem, c.stream)
+#define BUDE_LAUNCH(P, U) e = batch_launch_pu<P, U>(a, grid, cfg.wgsize, smem, st)
   BUDE_BATCH_DISPATCH(cfg, BUDE_LAUNCH)
 #undef BUDE_LAUNCH
   if (e != cudaSuccess) return cuda_error(e, "batch_kernel launch");
   c.launches++;
   if (a.split > 1 && n_items > 0) {
-    batch_reduce_kernel<<<(unsigned)n_items, 256, 0, c.stream>>>(items, partial, a.split, npose_space, energies);
+    batch_reduce_kernel<<<(unsigned)n_items, 256, 0, st>>>(items, partial, a.split, npose_space, energies);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "batch_reduce_kernel launch");
     c.launches++;
@@ -276,11 +278,13 @@ static int ensure_graph(Context &c, const bude_launch_cfg &cfg) {
 }
 
 int batch_items_enqueue(Context &c, const bude_launch_cfg &cfg, const int4 *items, int n_items, const float4 *xform,
-                        float *energies, float *partial, long long npose_space) {
+                        float *energies, float *partial, long long npose_space, cudaStream_t st,
+                        int max_blocks_per_sm) {
   int grid = 0;
   int rc = persistent_grid(c, cfg, &grid);
   if (rc) return rc;
-  return enqueue_items(c, cfg, grid, items, n_items, xform, energies, partial, npose_space);
+  if (max_blocks_per_sm > 0) grid = std::min(grid, max_blocks_per_sm * std::max(c.num_sms, 1));
+  return enqueue_items(c, cfg, grid, items, n_items, xform, energies, partial, npose_space, st);
 }
 
 int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand) {

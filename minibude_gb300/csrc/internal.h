@@ -81,13 +81,17 @@ void release_batch(Context &c);
 int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand);
 // Batch kernel over `items` (energies of the items' poses from the transforms at `xform`).  With
 // cfg.split > 1 the slice sums go through `partial` (at least cfg.split * npose_space floats) and a
-// slice reduction over pose indices [0, npose_space).
+// per-item slice reduction.  On stream `st` (nullptr: the context's stream); max_blocks_per_sm > 0
+// caps the persistent grid, leaving room on each SM for kernels running beside it.
 int batch_items_enqueue(Context &c, const bude_launch_cfg &cfg, const int4 *items, int n_items, const float4 *xform,
-                        float *energies, float *partial, long long npose_space);
+                        float *energies, float *partial, long long npose_space, cudaStream_t st = nullptr,
+                        int max_blocks_per_sm = 0);
 void release_surrogate(Context &c);
 void release_streamer(Context &c);
 void release_screen(Context &c);
 int surrogate_score_enqueue(Context &c, const float4 *xform_ready);
+int surrogate_prepare(Context &c, bool xform_ready);
+int surrogate_score_range(Context &c, int lig0, int lig1, int groups, cudaStream_t st);
 float *surrogate_scores(Context &c);
 int autotune(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms);
 int default_cfg(const Context &c, int ppwi, int wgsize, bude_launch_cfg &cfg);

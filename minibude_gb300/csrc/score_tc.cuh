@@ -1,6 +1,8 @@
 // score_tc.cuh -- surrogate inference on the 5th-generation tensor cores (tcgen05 + TMEM).
 //
-// A block runs kTcGroups independent tile groups of 128 threads.  A group scores one item at a
+// A block runs G independent tile groups of 128 threads (G = 4 for scoring alone; G = 3 leaves
+// shared memory and registers on each SM for exact-kernel blocks, which the screening pipeline
+// runs beside it).  A group scores one item at a
 // time: up to 128 poses of one ligand, pose r = thread r = TMEM lane r of the group's 128 TMEM
 // columns.  For every ligand atom the group
 //   1. builds each pose's 32 features (surrogate_kernels.cuh: features_of; the field channels
@@ -25,31 +27,34 @@
 
 namespace bude {
 
-constexpr int kTcGroups = 4;
+constexpr int kTcGroups = 4;         // tile groups per block when the scorer runs alone
 constexpr int kTcGroupThreads = 128; // warp w of a group reads TMEM lanes 32w .. 32w + 31
-constexpr int kTcThreads = kTcGroups * kTcGroupThreads;
 constexpr int kTcCols = 128;         // TMEM columns per group
 constexpr int kTcBiasK = 16;         // K of the bias UMMA (3 of 16 used)
 constexpr int kTcOutN = 16;          // N of the output UMMA (2 of 16 used)
 
-struct TcSmem {
+template <int G> struct TcSmem {
   alignas(128) unsigned char w1[kHid * kFeat * 2];          // W1: [128 out][32 in], K-major
   alignas(128) unsigned char w2[kHid * kHid * 2];           // W2
   alignas(128) unsigned char w3[kHid * kHid * 2];           // W3
   alignas(128) unsigned char bias[3][kHid * kTcBiasK * 2];  // b_l in three BF16 parts at k = 0..2
   alignas(128) unsigned char ones[kHid * kTcBiasK * 2];     // 1 at k = 0..2
   alignas(128) unsigned char w4[kTcOutN * kHid * 2];        // w4 in two BF16 parts at n = 0, 1
-  alignas(128) unsigned char act[kTcGroups][kHid * kHid * 2]; // per group: the layer input tile
+  alignas(128) unsigned char act[G][kHid * kHid * 2];         // per group: the layer input tile
   uint4 emb[kMaxTypes * 2];                                  // type embeddings (16 BF16 each)
-  alignas(8) uint64_t bar[kTcGroups];
+  alignas(8) uint64_t bar[G];
   uint32_t tmem;
 };
 
-static_assert(offsetof(TcSmem, w4) + sizeof(TcSmem::w4) - offsetof(TcSmem, bias) ==
-                  sizeof(TcSmem::bias) + sizeof(TcSmem::ones) + sizeof(TcSmem::w4),
+static_assert(offsetof(TcSmem<4>, w4) + sizeof(TcSmem<4>::w4) - offsetof(TcSmem<4>, bias) ==
+                  sizeof(TcSmem<4>::bias) + sizeof(TcSmem<4>::ones) + sizeof(TcSmem<4>::w4),
               "bias, ones and w4 tiles are contiguous (zeroed as one range)");
-static_assert(sizeof(TcSmem) <= 227 * 1024, "one block per SM fits the 227 KB shared-memory limit");
-static_assert(sizeof(TcSmem) > 114 * 1024, "shared memory keeps a second block (and its TMEM) off the SM");
+static_assert(sizeof(TcSmem<4>) <= 227 * 1024, "one block per SM fits the 227 KB shared-memory limit");
+// Every variant keeps a second scorer block (and its TMEM allocation) off an SM.
+static_assert(sizeof(TcSmem<3>) > 114 * 1024, "shared memory keeps a second scorer block off the SM");
+
+// TMEM columns a block allocates: a power of two covering G groups of 128.
+template <int G> __host__ __device__ constexpr int tc_alloc_cols() { return G * kTcCols <= 256 ? 256 : 512; }
 
 struct ScoreTcArgs {
   ScoreArgs s;
@@ -102,19 +107,20 @@ template <class Smem> __device__ __forceinline__ void tc_setup(Smem &s, const Ml
   }
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) score_tc_kernel(const ScoreTcArgs A) {
+template <int G>
+__global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const ScoreTcArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  TcSmem &s = *reinterpret_cast<TcSmem *>(smem_raw);
+  TcSmem<G> &s = *reinterpret_cast<TcSmem<G> *>(smem_raw);
   const ScoreArgs &a = A.s;
   const int tid = threadIdx.x, g = tid / kTcGroupThreads, lt = tid % kTcGroupThreads;
   const uint32_t bar_id = 1 + g; // named barrier of the group
 
   tc_setup(s, a.W);
   if (tid == 0) {
-    for (int q = 0; q < kTcGroups; ++q) mbar_init(&s.bar[q], 1);
+    for (int q = 0; q < G; ++q) mbar_init(&s.bar[q], 1);
     mbar_fence_init();
   }
-  if (tid < 32) tmem_alloc<kTcGroups * kTcCols>(&s.tmem);
+  if (tid < 32) tmem_alloc<tc_alloc_cols<G>()>(&s.tmem);
   fence_proxy_async();
   tc_fence_before();
   __syncthreads();
@@ -164,7 +170,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) score_tc_kernel(const ScoreTcAr
     named_sync(bar_id, kTcGroupThreads);
   };
 
-  for (int item = blockIdx.x * kTcGroups + g; item < a.n_items; item += gridDim.x * kTcGroups) {
+  for (int item = blockIdx.x * G + g; item < a.n_items; item += gridDim.x * G) {
     const int4 it = __ldg(&a.items[item]);
     const float4 *xf = a.xform + (long long)(it.z + min(lt, it.w - 1)) * 3;
     const float4 r0 = __ldg(xf), r1 = __ldg(xf + 1), r2 = __ldg(xf + 2);
@@ -223,7 +229,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) score_tc_kernel(const ScoreTcAr
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (tid < 32) tmem_dealloc<kTcGroups * kTcCols>(s.tmem);
+  if (tid < 32) tmem_dealloc<tc_alloc_cols<G>()>(s.tmem);
 }
 
 } // namespace bude

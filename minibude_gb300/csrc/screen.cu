@@ -4,8 +4,8 @@
 //   1. the surrogate scores all poses (surrogate.cu);
 //   2. select_kernel picks the top `top_frac` of poses by surrogate energy (lowest first; an exact
 //      radix select with ties taken in pose order, so the pick is deterministic) and an audit
-//      sample of about `audit_frac` of all poses, uniformly from the rest (a hash of the seed and
-//      the pose index decides);
+//      sample of exactly ceil(audit_frac * n) of the other poses, uniformly at random (the lowest
+//      seeded hashes of the pose indices);
 //   3. the picked poses are compacted and rescored by the exact kernel (batch_kernel over the
 //      compact transforms);
 //   4. audit_kernel measures the surrogate's ordering error on the audit sample,
@@ -68,90 +68,131 @@ __device__ __forceinline__ int block_scan(int v, int *warp_sums, int *total) {
   return before;
 }
 
-// Flags per pose: 1 = top pick, 2 = audit, 0 = neither.  counts[2l] = picks, counts[2l+1] = audit.
-__global__ void __launch_bounds__(kSelThreads) select_kernel(const float *scores, const long long *pose_off,
+// The counts select_kernel picks for a ligand of n poses; the host computes the same numbers (the
+// same float expressions) to lay out the rescoring before any kernel runs.
+__host__ __device__ inline int screen_top_count(float top_frac, int n) {
+  const int k = (int)ceilf(top_frac * (float)n);
+  return k < 0 ? 0 : (k > n ? n : k);
+}
+__host__ __device__ inline int screen_audit_count(float audit_frac, int n, int k) {
+  const int a = (int)ceilf(audit_frac * (float)n);
+  return a < 0 ? 0 : (a > n - k ? n - k : a);
+}
+
+// Radix select over the 32-bit keys key(i) of the eligible poses i < n (3 passes of 11/11/10 bits):
+// *thr = the need-th smallest key, *ties = how many of the keys equal to it are inside the pick.
+template <class Key>
+__device__ void radix_select(int n, int need, Key key, int *hist, uint32_t *s_prefix, uint32_t *s_mask, int *s_need,
+                             uint32_t *thr, int *ties) {
+  if (threadIdx.x == 0) {
+    *s_prefix = 0;
+    *s_mask = 0;
+    *s_need = need;
+  }
+  __syncthreads();
+  const int shifts[3] = {21, 10, 0};
+  const int widths[3] = {11, 11, 10};
+  for (int pass = 0; pass < 3 && need > 0; ++pass) {
+    const int sh = shifts[pass];
+    const uint32_t bm = (1u << widths[pass]) - 1u;
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    const uint32_t prefix = *s_prefix, mask = *s_mask;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      uint32_t k;
+      if (key(i, &k) && (k & mask) == prefix) atomicAdd(&hist[(k >> sh) & bm], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int left = *s_need, cum = 0;
+      uint32_t b = 0;
+      for (; b < bm; ++b) {
+        if (cum + hist[b] >= left) break;
+        cum += hist[b];
+      }
+      *s_need = left - cum;
+      *s_prefix = prefix | (b << sh);
+      *s_mask = mask | (bm << sh);
+    }
+    __syncthreads();
+  }
+  *thr = *s_prefix;
+  *ties = *s_need;
+  __syncthreads();
+}
+
+// Flags per pose: 1 = top pick, 2 = audit, 0 = neither.  Ligand l = lig0 + blockIdx.x.  The picks
+// are the screen_top_count lowest surrogate energies (ties in pose order); the audit sample is the
+// screen_audit_count other poses with the lowest seeded hash of their pose index (ties in pose
+// order), a uniform random sample of exactly that size.  counts[2l] = picks, counts[2l+1] = audit.
+__global__ void __launch_bounds__(kSelThreads) select_kernel(const float *scores, const long long *pose_off, int lig0,
                                                              float top_frac, float audit_frac, uint32_t seed,
                                                              unsigned char *flag, int *counts) {
   __shared__ int hist[2048];
   __shared__ int warp_sums[32];
   __shared__ uint32_t s_prefix, s_mask;
   __shared__ int s_need;
-  const int l = blockIdx.x;
+  const int l = lig0 + blockIdx.x;
   const long long off = pose_off[l];
   const int n = (int)(pose_off[l + 1] - off);
-  int k = (int)ceilf(top_frac * (float)n);
-  k = max(0, min(n, k));
-  if (threadIdx.x == 0) {
-    s_prefix = 0;
-    s_mask = 0;
-    s_need = k;
-  }
-  __syncthreads();
-  const int shifts[3] = {21, 10, 0};
-  const int widths[3] = {11, 11, 10};
-  for (int pass = 0; pass < 3 && k > 0; ++pass) {
-    const int sh = shifts[pass];
-    const uint32_t bm = (1u << widths[pass]) - 1u;
-    for (int i = threadIdx.x; i < 2048; i += blockDim.x) hist[i] = 0;
-    __syncthreads();
-    const uint32_t prefix = s_prefix, mask = s_mask;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      const uint32_t key = order_key(scores[off + i]);
-      if ((key & mask) == prefix) atomicAdd(&hist[(key >> sh) & bm], 1);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int need = s_need, cum = 0;
-      uint32_t b = 0;
-      for (; b < bm; ++b) {
-        if (cum + hist[b] >= need) break;
-        cum += hist[b];
-      }
-      s_need = need - cum;
-      s_prefix = prefix | (b << sh);
-      s_mask = mask | (bm << sh);
-    }
-    __syncthreads();
-  }
-  const uint32_t T = s_prefix; // key of the k-th smallest score
-  const int ties_needed = s_need;
-  // Flags in pose order: keys < T, then the first `ties_needed` keys == T.
-  const uint32_t audit_thr =
-      (uint32_t)fminf(4294967295.f, 4294967296.f * (k < n ? audit_frac * n / (float)(n - k) : 0.f));
-  int tie_base = 0, audit_count = 0;
+  const int k = screen_top_count(top_frac, n);
+  const int ka = screen_audit_count(audit_frac, n, k);
+  uint32_t T = 0, Ta = 0;
+  int ties = 0, ties_a = 0;
+  // 1. the picks: keys below T, then the first `ties` keys equal to T in pose order
+  radix_select(
+      n, k,
+      [&](int i, uint32_t *key) {
+        *key = order_key(scores[off + i]);
+        return true;
+      },
+      hist, &s_prefix, &s_mask, &s_need, &T, &ties);
+  int tie_base = 0;
   for (int c0 = 0; c0 < n; c0 += blockDim.x) {
     const int i = c0 + threadIdx.x;
-    uint32_t key = 0xffffffffu;
-    if (i < n) key = order_key(scores[off + i]);
+    const uint32_t key = i < n ? order_key(scores[off + i]) : 0xffffffffu;
     const int is_tie = (k > 0 && i < n && key == T) ? 1 : 0;
     int tot = 0;
     const int rank = block_scan(is_tie, warp_sums, &tot);
-    if (i < n) {
-      unsigned char f = 0;
-      if (k > 0 && (key < T || (is_tie && tie_base + rank < ties_needed))) f = 1;
-      else if (mix_hash(seed, (uint32_t)(off + i)) < audit_thr) f = 2;
-      flag[off + i] = f;
-      audit_count += (f == 2);
-    }
+    if (i < n) flag[off + i] = (k > 0 && (key < T || (is_tie && tie_base + rank < ties))) ? 1 : 0;
     tie_base += tot;
   }
-  // block sum of audit picks
-  int tot = 0;
-  (void)block_scan(audit_count, warp_sums, &tot);
+  __threadfence_block();
+  __syncthreads();
+  // 2. the audit sample among the other poses
+  radix_select(
+      n, ka,
+      [&](int i, uint32_t *key) {
+        *key = mix_hash(seed, (uint32_t)(off + i));
+        return flag[off + i] == 0;
+      },
+      hist, &s_prefix, &s_mask, &s_need, &Ta, &ties_a);
+  tie_base = 0;
+  for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+    const int i = c0 + threadIdx.x;
+    const bool free_pose = i < n && flag[off + i] == 0;
+    const uint32_t h = free_pose ? mix_hash(seed, (uint32_t)(off + i)) : 0xffffffffu;
+    const int is_tie = (ka > 0 && free_pose && h == Ta) ? 1 : 0;
+    int tot = 0;
+    const int rank = block_scan(is_tie, warp_sums, &tot);
+    if (free_pose && ka > 0 && (h < Ta || (is_tie && tie_base + rank < ties_a))) flag[off + i] = 2;
+    tie_base += tot;
+  }
   if (threadIdx.x == 0) {
     counts[2 * l] = k;
-    counts[2 * l + 1] = tot;
+    counts[2 * l + 1] = ka;
   }
 }
 
 // Write the picked poses of ligand l (picks first, then audit, each in pose order) from
 // comp_off[l] on, and gather their transforms.
-__global__ void __launch_bounds__(kSelThreads) compact_kernel(const long long *pose_off, const unsigned char *flag,
+__global__ void __launch_bounds__(kSelThreads) compact_kernel(const long long *pose_off, int lig0,
+                                                              const unsigned char *flag,
                                                               const long long *comp_off, const int *counts,
                                                               const float4 *xform, int *comp_pose,
                                                               float4 *comp_xform) {
   __shared__ int warp_sums[32];
-  const int l = blockIdx.x;
+  const int l = lig0 + blockIdx.x;
   const long long off = pose_off[l];
   const int n = (int)(pose_off[l + 1] - off);
   const long long base = comp_off[l];
@@ -253,7 +294,8 @@ __global__ void fallback_copy_kernel(const long long *pose_off, const int *fallb
 
 struct ScreenState {
   DevBuf pose_off, flag, counts, comp_off, comp_pose, comp_xform, comp_exact, err, final_e, rescored, items, fb;
-  DevBuf partial; // slice sums of split exact evaluations
+  DevBuf partial;             // slice sums of split exact evaluations
+  cudaStream_t side = nullptr; // the exact rescoring beside the surrogate
 };
 
 void release_screen(Context &c) {
@@ -262,6 +304,7 @@ void release_screen(Context &c) {
   for (DevBuf *b : {&s.pose_off, &s.flag, &s.counts, &s.comp_off, &s.comp_pose, &s.comp_xform, &s.comp_exact,
                     &s.err, &s.final_e, &s.rescored, &s.items, &s.fb, &s.partial})
     b->release();
+  if (s.side) cudaStreamDestroy(s.side);
   delete c.screen;
   c.screen = nullptr;
 }
@@ -321,56 +364,107 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
   cfg.cluster = 0;
   rc = check_cfg(c, cfg);
   if (rc) return rc;
-  cudaEvent_t ev[5];
-  for (auto &e : ev) cudaEventCreate(&e);
-  cudaEventRecord(ev[0], c.stream);
-  cudaMemcpyAsync(s.pose_off.ptr, c.pose_off.data(), (size_t)(nl + 1) * 8, cudaMemcpyHostToDevice, c.stream);
-  // 1. surrogate over every pose (computes the pose transforms first)
-  rc = surrogate_score_enqueue(c, nullptr);
-  if (rc) return rc;
-  const float *scores = surrogate_scores(c);
-  cudaEventRecord(ev[1], c.stream);
-  // 2. picks and audit sample
-  if (nl > 0)
-    select_kernel<<<nl, kSelThreads, 0, c.stream>>>(scores, s.pose_off.as<long long>(), sc.top_frac, sc.audit_frac,
-                                                    (uint32_t)sc.seed, s.flag.as<unsigned char>(), s.counts.as<int>());
-  c.launches += nl > 0;
+  // The picks and audit counts per ligand depend only on its pose count, so the compacted layout
+  // and the rescoring items are known before any kernel runs.
   std::vector<int> counts((size_t)2 * nl);
-  if (nl > 0) cudaMemcpyAsync(counts.data(), s.counts.ptr, counts.size() * 4, cudaMemcpyDeviceToHost, c.stream);
-  cudaError_t e = cudaStreamSynchronize(c.stream);
-  if (e != cudaSuccess) return cuda_error(e, "screen selection");
   std::vector<long long> comp_off((size_t)nl + 1, 0);
-  for (int l = 0; l < nl; ++l) comp_off[l + 1] = comp_off[l] + counts[2 * l] + counts[2 * l + 1];
+  for (int l = 0; l < nl; ++l) {
+    const int n = (int)(c.pose_off[l + 1] - c.pose_off[l]);
+    counts[2 * l] = screen_top_count(sc.top_frac, n);
+    counts[2 * l + 1] = screen_audit_count(sc.audit_frac, n, counts[2 * l]);
+    comp_off[l + 1] = comp_off[l] + counts[2 * l] + counts[2 * l + 1];
+  }
   const long long ncomp = comp_off[nl];
   rc = s.comp_pose.reserve((size_t)std::max(ncomp, 1LL) * 4, "compact poses");
   if (!rc) rc = s.comp_xform.reserve((size_t)std::max(ncomp, 1LL) * 48, "compact transforms");
   if (!rc) rc = s.comp_exact.reserve((size_t)std::max(ncomp, 1LL) * 4, "compact energies");
+  if (!rc && cfg.split > 1)
+    rc = s.partial.reserve((size_t)cfg.split * (size_t)std::max(ncomp, 1LL) * sizeof(float), "screen slice sums");
   if (rc) return rc;
-  cudaMemcpyAsync(s.comp_off.ptr, comp_off.data(), comp_off.size() * 8, cudaMemcpyHostToDevice, c.stream);
-  if (nl > 0)
-    compact_kernel<<<nl, kSelThreads, 0, c.stream>>>(s.pose_off.as<long long>(), s.flag.as<unsigned char>(),
-                                                     s.comp_off.as<long long>(), s.counts.as<int>(),
-                                                     c.b_xform.as<float4>(), s.comp_pose.as<int>(),
-                                                     s.comp_xform.as<float4>());
-  c.launches += nl > 0;
-  // 3. exact rescoring of picks + audit
-  std::vector<int> lig, cnt;
-  std::vector<long long> first;
-  for (int l = 0; l < nl; ++l) {
-    const int k = counts[2 * l] + counts[2 * l + 1];
-    if (k == 0) continue;
-    lig.push_back(l);
-    first.push_back(comp_off[l]);
-    cnt.push_back(k);
-  }
-  // Each ligand contributes only a few hundred picks: rescore them in 256-pose items so blocks are
+  // Ligand chunks (sc.chunks > 1): the surrogate scores chunk j+1 (3 tile groups per block) while
+  // the exact kernel rescores chunk j's picks beside it on a second stream, two blocks per SM.
+  // Measured on 1,024 ligands x 16,384 poses it is slower (126 ms against 106 ms): the rescoring
+  // blocks slow the scorer more than they hide, so one chunk (no overlap, 4 groups) is the default.
+  const int nchunks = nl == 0 ? 0 : std::max(1, std::min(nl, sc.chunks > 0 ? sc.chunks : 1));
+  const bool overlap = nchunks > 1;
+  // Each ligand contributes only a few hundred picks: rescore them in small items so blocks are
   // not mostly empty, with the fallback's protein slices (the pose shape does not change the
   // arithmetic of a pose, the slices do).
-  const bude_launch_cfg small{4, 64, cfg.split, cfg.tile, 2, 0};
-  rc = run_items(c, s, small, range_items(c, lig, first, cnt, small.ppwi * small.wgsize), s.comp_xform.as<float4>(),
-                 s.comp_exact.as<float>(), ncomp);
+  const bude_launch_cfg small = overlap ? bude_launch_cfg{4, 128, cfg.split, cfg.tile, 2, 0}
+                                        : bude_launch_cfg{4, 64, cfg.split, cfg.tile, 2, 0};
+  std::vector<int> chunk_lig(nchunks + 1, nl), chunk_item(nchunks + 1, 0);
+  std::vector<int4> items;
+  for (int j = 0; j < nchunks; ++j) {
+    chunk_lig[j] = (int)((long long)nl * j / nchunks);
+    std::vector<int> lig, cnt;
+    std::vector<long long> first;
+    for (int l = (int)((long long)nl * j / nchunks); l < (int)((long long)nl * (j + 1) / nchunks); ++l) {
+      const int k = counts[2 * l] + counts[2 * l + 1];
+      if (k == 0) continue;
+      lig.push_back(l);
+      first.push_back(comp_off[l]);
+      cnt.push_back(k);
+    }
+    chunk_item[j] = (int)items.size();
+    const std::vector<int4> its = range_items(c, lig, first, cnt, small.ppwi * small.wgsize);
+    items.insert(items.end(), its.begin(), its.end());
+  }
+  if (nchunks > 0) chunk_item[nchunks] = (int)items.size();
+  rc = s.items.reserve(std::max<size_t>(items.size(), 1) * sizeof(int4), "screen items");
   if (rc) return rc;
+  if (overlap && !s.side) {
+    cudaError_t es = cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking);
+    if (es != cudaSuccess) return cuda_error(es, "screen rescoring stream");
+  }
+  std::vector<cudaEvent_t> ready(nchunks);
+  for (auto &x : ready) cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+  cudaEvent_t ev[5];
+  for (auto &e : ev) cudaEventCreate(&e);
+  cudaEventRecord(ev[0], c.stream);
+  cudaEventRecord(ev[1], c.stream); // re-recorded after each chunk's surrogate
+  cudaMemcpyAsync(s.pose_off.ptr, c.pose_off.data(), (size_t)(nl + 1) * 8, cudaMemcpyHostToDevice, c.stream);
+  cudaMemcpyAsync(s.comp_off.ptr, comp_off.data(), comp_off.size() * 8, cudaMemcpyHostToDevice, c.stream);
+  if (!items.empty())
+    cudaMemcpyAsync(s.items.ptr, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, c.stream);
+  rc = surrogate_prepare(c, false); // pose transforms of every pose
+  if (rc) return rc;
+  const float *scores = surrogate_scores(c);
+  cudaStream_t rs = overlap ? s.side : c.stream;
+  // 1-3. per chunk: surrogate, picks and audit sample, compaction; exact rescoring on `rs`
+  for (int j = 0; j < nchunks && !rc; ++j) {
+    const int l0 = chunk_lig[j], l1 = chunk_lig[j + 1];
+    rc = surrogate_score_range(c, l0, l1, overlap ? 3 : 4, c.stream);
+    if (rc) break;
+    cudaEventRecord(ev[1], c.stream); // after the last chunk's surrogate: the end of the surrogate phase
+    if (l1 > l0) {
+      select_kernel<<<l1 - l0, kSelThreads, 0, c.stream>>>(scores, s.pose_off.as<long long>(), l0, sc.top_frac,
+                                                           sc.audit_frac, (uint32_t)sc.seed,
+                                                           s.flag.as<unsigned char>(), s.counts.as<int>());
+      compact_kernel<<<l1 - l0, kSelThreads, 0, c.stream>>>(s.pose_off.as<long long>(), l0,
+                                                            s.flag.as<unsigned char>(), s.comp_off.as<long long>(),
+                                                            s.counts.as<int>(), c.b_xform.as<float4>(),
+                                                            s.comp_pose.as<int>(), s.comp_xform.as<float4>());
+      c.launches += 2;
+    }
+    cudaEventRecord(ready[j], c.stream);
+    if (overlap) cudaStreamWaitEvent(rs, ready[j], 0);
+    const int n_it = chunk_item[j + 1] - chunk_item[j];
+    if (n_it > 0)
+      rc = batch_items_enqueue(c, small, s.items.as<int4>() + chunk_item[j], n_it, s.comp_xform.as<float4>(),
+                               s.comp_exact.as<float>(), s.partial.as<float>(), ncomp, rs, overlap ? 2 : 0);
+  }
+  if (overlap) {
+    cudaEvent_t joined = ready.empty() ? nullptr : ready[0];
+    if (joined) {
+      cudaEventRecord(joined, rs);
+      cudaStreamWaitEvent(c.stream, joined, 0);
+    }
+  }
   cudaEventRecord(ev[2], c.stream);
+  cudaError_t e = cudaStreamSynchronize(c.stream);
+  for (auto &x : ready) cudaEventDestroy(x);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_error(e, "screen rescoring");
   // 4. audit and fallback
   if (nl > 0)
     audit_kernel<<<nl, 256, 0, c.stream>>>(s.comp_off.as<long long>(), s.counts.as<int>(), s.comp_pose.as<int>(),

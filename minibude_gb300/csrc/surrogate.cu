@@ -53,6 +53,7 @@ struct Surrogate {
   long long rows_cap = 0;
   // scoring
   DevBuf items, scores;
+  std::vector<int> item_lig_off; // nligands + 1: first scoring item of each ligand
   int items_for = 0;
   int n_items = 0;
   int scorer = BUDE_SCORER_TCGEN05;
@@ -123,7 +124,9 @@ static int set_smem_limits() {
   if (done) return BUDE_OK;
   cudaError_t e = cudaFuncSetAttribute(score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(score_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem));
+    e = cudaFuncSetAttribute(score_tc_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem<4>));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(score_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem<3>));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(train_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
   if (e == cudaSuccess)
@@ -608,8 +611,9 @@ int surrogate_features(Context &c, const int *poses, int n, float *X, int *types
   return BUDE_OK;
 }
 
-// Surrogate energies of every pose of the uploaded batch into s.scores (device).
-int surrogate_score_enqueue(Context &c, const float4 *xform_ready) {
+// Scoring items (128 poses of one ligand each, ligand by ligand) and, unless the caller already
+// computed them, the pose transforms of the uploaded batch.
+int surrogate_prepare(Context &c, bool xform_ready) {
   Surrogate &s = sur(c);
   if (!s.ready) return set_error(BUDE_ERR_STATE, "surrogate not initialised");
   if (!c.have_batch) return set_error(BUDE_ERR_STATE, "no batch uploaded");
@@ -617,12 +621,15 @@ int surrogate_score_enqueue(Context &c, const float4 *xform_ready) {
   const long long np = c.batch_poses;
   int rc = s.scores.reserve((size_t)std::max(np, 1LL) * 4, "surrogate scores");
   if (rc) return rc;
-  if (s.items_for != (int)np || s.n_items == 0) {
+  if (s.items_for != (int)np || (int)s.item_lig_off.size() != c.nligands + 1) {
     std::vector<int4> items;
-    for (int l = 0; l < c.nligands; ++l)
+    s.item_lig_off.assign(1, 0);
+    for (int l = 0; l < c.nligands; ++l) {
       for (long long p = c.pose_off[l]; p < c.pose_off[l + 1]; p += kRowsPerCta)
         items.push_back(make_int4(c.lig_off[l], c.lig_off[l + 1] - c.lig_off[l], (int)p,
                                   (int)std::min<long long>(kRowsPerCta, c.pose_off[l + 1] - p)));
+      s.item_lig_off.push_back((int)items.size());
+    }
     rc = s.items.reserve(std::max<size_t>(items.size(), 1) * sizeof(int4), "surrogate items");
     if (rc) return rc;
     if (!items.empty()) cudaMemcpy(s.items.ptr, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice);
@@ -633,37 +640,52 @@ int surrogate_score_enqueue(Context &c, const float4 *xform_ready) {
     rc = batch_transforms(c);
     if (rc) return rc;
   }
-  if (s.n_items == 0) return BUDE_OK;
-  rc = set_smem_limits();
-  if (rc) return rc;
+  return set_smem_limits();
+}
+
+// Surrogate energies of the poses of ligands [lig0, lig1) into s.scores, on `st`.  The tcgen05
+// scorer runs `groups` tile groups per block (4 alone; 3 leaves room for exact-kernel blocks).
+int surrogate_score_range(Context &c, int lig0, int lig1, int groups, cudaStream_t st) {
+  Surrogate &s = sur(c);
+  const int i0 = s.item_lig_off[lig0], n_items = s.item_lig_off[lig1] - i0;
+  if (n_items <= 0) return BUDE_OK;
   ScoreArgs a;
   a.W = weights(s);
   a.g = s.fg;
   a.ligands = c.b_ligands.as<float4>();
   a.xform = c.b_xform.as<float4>();
-  a.items = s.items.as<int4>();
+  a.items = s.items.as<int4>() + i0;
   a.scores = s.scores.as<float>();
-  a.n_items = s.n_items;
+  a.n_items = n_items;
   int per_sm = 0;
   cudaError_t e;
   if (s.scorer == BUDE_SCORER_TCGEN05) {
     ScoreTcArgs t;
     t.s = a;
     t.err = c.err.as<unsigned int>();
-    // One block per SM: a block holds all 512 TMEM columns of its SM.
-    const int grid = std::min((s.n_items + kTcGroups - 1) / kTcGroups, std::max(c.num_sms, 1));
-    score_tc_kernel<<<grid, kTcThreads, sizeof(TcSmem), c.stream>>>(t);
+    // One block per SM: a block holds all of its SM's TMEM it allocates.
+    const int g = groups == 3 ? 3 : 4;
+    const int grid = std::min((n_items + g - 1) / g, std::max(c.num_sms, 1));
+    if (g == 3) score_tc_kernel<3><<<grid, 3 * kTcGroupThreads, sizeof(TcSmem<3>), st>>>(t);
+    else score_tc_kernel<4><<<grid, 4 * kTcGroupThreads, sizeof(TcSmem<4>), st>>>(t);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "score_tc_kernel launch");
   } else {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, score_kernel, kMlpThreads, sizeof(MlpSmem));
-    const int grid = std::min(s.n_items, std::max(1, per_sm) * std::max(c.num_sms, 1));
-    score_kernel<<<grid, kMlpThreads, sizeof(MlpSmem), c.stream>>>(a);
+    const int grid = std::min(n_items, std::max(1, per_sm) * std::max(c.num_sms, 1));
+    score_kernel<<<grid, kMlpThreads, sizeof(MlpSmem), st>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "score_kernel launch");
   }
   c.launches++;
   return BUDE_OK;
+}
+
+// Surrogate energies of every pose of the uploaded batch into s.scores (device).
+int surrogate_score_enqueue(Context &c, const float4 *xform_ready) {
+  int rc = surrogate_prepare(c, xform_ready != nullptr);
+  if (!rc) rc = surrogate_score_range(c, 0, c.nligands, kTcGroups, c.stream);
+  return rc;
 }
 
 float *surrogate_scores(Context &c) { return c.surrogate ? c.surrogate->scores.as<float>() : nullptr; }

@@ -184,3 +184,28 @@ def test_surrogate_errors(built_library):
         big_ff = np.concatenate([ff, ff, ff])
         with pytest.raises(BudeError):
             ctx.surrogate_init(protein, big_ff)  # 102 types > 64
+
+
+def test_screen_chunks_give_the_same_answer(built_library):
+    # The ligand-chunk pipeline (rescoring beside the surrogate on a second stream) changes the
+    # schedule, not the result; the audit sample has exactly ceil(audit_frac * n) poses.
+    protein, ff = small_protein()
+    batch = synthetic_batch(BatchSpec("t", 24, 16, 64, 300, 2000), protein, ff, 13)
+    with GpuContext(0) as ctx:
+        ctx.upload_batch(batch)
+        ctx.surrogate_init(protein, ff, seed=2)
+        ctx.surrogate_train(2, batch_poses=1024, lr=2e-3, seed=3)
+        out = []
+        for chunks in (1, 5):
+            st = ctx.screen(launch_cfg(8, 128, 4, 64, 2, cluster=0), top_frac=0.02, audit_frac=0.05, audit_tol=1e9,
+                            seed=5, chunks=chunks)
+            out.append((st, ctx.screen_download(batch.nligands)))
+        (st1, (f1, r1, e1)), (st5, (f5, r5, e5)) = out
+        assert np.array_equal(f1, f5) and np.array_equal(r1, r5) and np.array_equal(e1, e5)
+        off = batch.pose_offsets()
+        want = 0
+        for l in range(batch.nligands):
+            n = int(off[l + 1] - off[l])
+            k = min(n, int(np.ceil(np.float32(0.02) * np.float32(n))))
+            want += k + min(n - k, int(np.ceil(np.float32(0.05) * np.float32(n))))
+        assert st1["rescored_poses"] == st5["rescored_poses"] == want == r1.sum()
