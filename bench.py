@@ -62,6 +62,8 @@ def parse_args():
                     help="screen workload: load the trained surrogate from this file if it exists, else train and "
                          "save it there")
     ap.add_argument("--cfg", default="auto", help="auto, or ppwi,wgsize,split,tile[,unroll]")
+    ap.add_argument("--batch-ligands", type=int, default=0,
+                    help="batch workload: score only the first N of its 256 ligands (profiling cases)")
     ap.add_argument("--nposes", type=int, default=0, help="use the first N poses of the deck (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -341,10 +343,16 @@ def run_batch(args, dist: Dist):
     build.build_library()
     protein, ff = bm2_protein()
     batch = synthetic_batch(BATCH, protein, ff, seed=dist.rank)
+    if args.batch_ligands:
+        batch = batch.subset(range(min(args.batch_ligands, batch.nligands)))
     peaks = measured_peaks()
     ctx = GpuContext(dist.local_rank)
     ctx.upload_batch(batch)
-    cfg, _ = ctx.autotune_batch()
+    if args.cfg != "auto":
+        from minibude_gb300.model import launch_cfg
+        cfg = launch_cfg(*[int(x) for x in args.cfg.split(",")])
+    else:
+        cfg, _ = ctx.autotune_batch()
     for _ in range(max(args.warmup, 1)):
         ctx.run_batch(cfg)
     launches0 = ctx.launch_count()
@@ -382,7 +390,7 @@ def run_batch(args, dist: Dist):
                         "frac": round(achieved / peak, 4), "kernel": "batch_kernel",
                         "work": "30 FLOP/interaction + 18/(pose, ligand atom) + 28/pose (src/main.cpp:359)",
                         "peak_source": f"{sms} SMs x 128 x 2 x {sm_max:.0f} MHz (nominal at sm_max_mhz)",
-                        "traffic": None}}
+                        "traffic": traffic_per_launch(batch.total_poses, "batch_kernel")}}
     if not args.no_e2e:
         ts = []
         for i in range(args.warmup + max(2, args.steps // 2)):
