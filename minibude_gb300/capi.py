@@ -47,7 +47,8 @@ class BudeLaunchCfg(ctypes.Structure):
 
 class BudeScreenCfg(ctypes.Structure):
     _fields_ = [("top_frac", ctypes.c_float), ("audit_frac", ctypes.c_float), ("audit_tol", ctypes.c_float),
-                ("seed", ctypes.c_uint32), ("exact", BudeLaunchCfg), ("chunks", c_int32)]
+                ("seed", ctypes.c_uint32), ("exact", BudeLaunchCfg), ("chunks", c_int32),
+                ("rescore", BudeLaunchCfg)]
 
 
 class BudeScreenStats(ctypes.Structure):

@@ -389,9 +389,20 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
   const bool overlap = nchunks > 1;
   // Each ligand contributes only a few hundred picks: rescore them in small items so blocks are
   // not mostly empty, with the fallback's protein slices (the pose shape does not change the
-  // arithmetic of a pose, the slices do).
-  const bude_launch_cfg small = overlap ? bude_launch_cfg{4, 128, cfg.split, cfg.tile, 2, 0}
-                                        : bude_launch_cfg{4, 64, cfg.split, cfg.tile, 2, 0};
+  // arithmetic of a pose, the slices do).  One-warp blocks of 8 poses per thread (256-pose
+  // items) measured fastest on 410 picks per ligand (8 slices: 27.9 ms against 30.5 for 64
+  // threads x 4 poses); fewer picks per ligand get 128-pose items.
+  int with_picks = 0;
+  for (int l = 0; l < nl; ++l) with_picks += counts[2 * l] + counts[2 * l + 1] > 0;
+  const long long per_lig = with_picks ? ncomp / with_picks : 0;
+  bude_launch_cfg small = overlap         ? bude_launch_cfg{4, 128, cfg.split, cfg.tile, 2, 0}
+                          : per_lig >= 128 ? bude_launch_cfg{8, 32, cfg.split, cfg.tile, 4, 0}
+                                           : bude_launch_cfg{4, 32, cfg.split, cfg.tile, 2, 0};
+  if (sc.rescore.ppwi != 0) {
+    small = bude_launch_cfg{sc.rescore.ppwi, sc.rescore.wgsize, cfg.split, cfg.tile, sc.rescore.unroll, 0};
+    rc = check_cfg(c, small);
+    if (rc) return rc;
+  }
   std::vector<int> chunk_lig(nchunks + 1, nl), chunk_item(nchunks + 1, 0);
   std::vector<int4> items;
   for (int j = 0; j < nchunks; ++j) {

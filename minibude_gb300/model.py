@@ -230,10 +230,13 @@ class GpuContext:
 
     # -- screening -------------------------------------------------------------------------------
     def screen(self, exact_cfg: BudeLaunchCfg, top_frac: float = 0.02, audit_frac: float = 0.005,
-               audit_tol: float = 0.05, seed: int = 1, chunks: int = 0) -> dict:
+               audit_tol: float = 0.05, seed: int = 1, chunks: int = 0,
+               rescore_cfg: Optional[BudeLaunchCfg] = None) -> dict:
         """Surrogate-screened scoring of the uploaded batch (bude_screen_run); chunks = ligand
-        chunks of the surrogate / exact-rescoring pipeline (0: automatic)."""
-        cfg = BudeScreenCfg(top_frac, audit_frac, audit_tol, seed, exact_cfg, chunks)
+        chunks of the surrogate / exact-rescoring pipeline (0: automatic); rescore_cfg = pose shape
+        (ppwi, wgsize, unroll) of the exact rescoring (None: chosen by the library)."""
+        cfg = BudeScreenCfg(top_frac, audit_frac, audit_tol, seed, exact_cfg, chunks,
+                            rescore_cfg if rescore_cfg is not None else BudeLaunchCfg())
         st = BudeScreenStats()
         check(self._lib.bude_screen_run(self.handle, ctypes.byref(cfg), ctypes.byref(st)))
         return st.as_dict()
