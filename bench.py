@@ -364,8 +364,17 @@ def run_batch(args, dist: Dist):
     clk = clocks.summary(peaks.get("sm_max_mhz", 2070.0))
     step_ms = dist.max(float(np.mean(ms)))
     inter = batch.interactions
-    ctx.run_batch(cfg, per_ligand=True)
-    ms_pl = [ctx.run_batch(cfg, per_ligand=True) for _ in range(max(2, args.steps // 2))]
+    # One plain launch per ligand, at the best of a few shapes: the batch's own, and shapes that
+    # cut each ligand's launch into more blocks (fewer poses per block, protein slices).
+    from minibude_gb300.model import launch_cfg as _lc
+    pl_cands = [cfg, _lc(8, 128, 1, 64, 2), _lc(4, 128, 4, 64, 2, cluster=0), _lc(16, 128, 8, 64, 1, cluster=0),
+                _lc(8, 64, 4, 64, 2, cluster=1)]
+    pl_t = []
+    for c in pl_cands:
+        ctx.run_batch(c, per_ligand=True)
+        pl_t.append(ctx.run_batch(c, per_ligand=True))
+    pl_cfg = pl_cands[int(np.argmin(pl_t))]
+    ms_pl = [ctx.run_batch(pl_cfg, per_ligand=True) for _ in range(max(2, args.steps // 2))]
     pl_ms = float(np.mean(ms_pl))
     sms = _sm_count(dist.local_rank)
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
@@ -382,7 +391,8 @@ def run_batch(args, dist: Dist):
                       "mode": "one persistent kernel in a CUDA graph (counter reset + transforms + kernel)",
                       "per_ligand": {"ms_per_step": round(pl_ms, 4),
                                      "value": round(inter / (pl_ms * 1e-3) / 1e9, 3),
-                                     "launches_per_step": 1 + batch.nligands},
+                                     "launches_per_step": 1 + batch.nligands, "launch": pl_cfg.as_dict(),
+                                     "shapes_tried": len(pl_cands)},
                       "l2": "inputs (slab 11 MB, poses 129 MB, transforms 258 MB) exceed L2",
                       "parallelism": f"replicas x{dist.world}"},
            "gpu_launches": launches, "clocks": clk,

@@ -331,7 +331,9 @@ int autotune_batch(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms
     return BUDE_OK;
   }
   struct Shape { int p, w, u; };
-  const Shape shapes[] = {{16, 128, 1}, {16, 256, 1}, {8, 128, 2}, {8, 64, 2}, {8, 256, 2}, {4, 128, 4}};
+  // Short items run with P/2 or P/4 poses per thread, so P = 16 no longer loses a ligand's last
+  // pose block to padding and leads the list.
+  const Shape shapes[] = {{16, 128, 1}, {16, 256, 1}, {16, 64, 1}, {8, 128, 2}, {8, 64, 2}, {8, 256, 2}};
   // Time each shape on every k-th item of its own item list so one timing covers about 2e10
   // interactions (the mix of ligand sizes is kept) while still giving every resident block slot
   // at least 8 items (a subset smaller than the grid would time latency, not throughput).

@@ -103,40 +103,49 @@ __global__ void __launch_bounds__(kMaxThreads) batch_kernel(const BatchArgs a) {
     if (tid == 0)
       for (int q = 0; q < min(kStages - 1, Q); ++q) issue(q);
 
-    PosePairs<P> pp;
-    pp.clear();
-    int q = 0;
-    for (; q < Q; ++q) {
-      const int il = q / ntile;
-      const int k = q - il * ntile;
-      if (k == 0) pp.transform(__ldg(&lig[il]), a.xform, base, nthr, end);
-      if (__syncthreads_or(failed)) break;
-      if (tid == 0 && q + kStages - 1 < Q) issue(q + kStages - 1);
-      const long long step = qg + q;
-      const int s = (int)(step % kStages);
-      if (!mbar_wait_bounded(&full[s], (uint32_t)(step / kStages) & 1u)) {
-        failed = true;
-        continue;
+    // The last item of a ligand is usually short: an item that fits in P/2 or P/4 poses per thread
+    // runs with that many (a pose's arithmetic does not depend on the poses per thread).
+    auto run = [&](auto pp) -> bool {
+      pp.clear();
+      int q = 0;
+      for (; q < Q; ++q) {
+        const int il = q / ntile;
+        const int k = q - il * ntile;
+        if (k == 0) pp.transform(__ldg(&lig[il]), a.xform, base, nthr, end);
+        if (__syncthreads_or(failed)) break;
+        if (tid == 0 && q + kStages - 1 < Q) issue(q + kStages - 1);
+        const long long step = qg + q;
+        const int s = (int)(step % kStages);
+        if (!mbar_wait_bounded(&full[s], (uint32_t)(step / kStages) & 1u)) {
+          failed = true;
+          continue;
+        }
+        pp.template tile<U>(stages + (size_t)s * a.tile * kRecF4, min(a.tile, a1 - (a0 + k * a.tile)));
       }
-      pp.template tile<U>(stages + (size_t)s * a.tile * kRecF4, min(a.tile, a1 - (a0 + k * a.tile)));
-    }
-    const bool ok = !__syncthreads_or(failed || q < Q);
-    if (!ok) {
-      if (tid == 0) {
-        // Record the timeout and wait (bounded) for this block's copies still in flight.
-        atomicOr(a.err, 1u);
-        for (int d = max(0, q - 1); d < min(Q, q + kStages - 1); ++d)
-          (void)mbar_wait_bounded(&full[(qg + d) % kStages], (uint32_t)((qg + d) / kStages) & 1u);
+      const bool ok = !__syncthreads_or(failed || q < Q);
+      if (!ok) {
+        if (tid == 0) {
+          // Record the timeout and wait (bounded) for this block's copies still in flight.
+          atomicOr(a.err, 1u);
+          for (int d = max(0, q - 1); d < min(Q, q + kStages - 1); ++d)
+            (void)mbar_wait_bounded(&full[(qg + d) % kStages], (uint32_t)((qg + d) / kStages) & 1u);
+        }
+        return false;
       }
-      return;
-    }
-    float *out = a.split > 1 ? a.partial + (long long)sl * a.npose_space : a.energies;
-    const float scale = a.split > 1 ? 1.f : 0.5f;
+      float *out = a.split > 1 ? a.partial + (long long)sl * a.npose_space : a.energies;
+      const float scale = a.split > 1 ? 1.f : 0.5f;
 #pragma unroll
-    for (int i = 0; i < P; ++i) {
-      const long long pi = base + (long long)i * nthr;
-      if (pi < end) out[pi] = scale * pp.energy(i);
-    }
+      for (int i = 0; i < decltype(pp)::kP; ++i) {
+        const long long pi = base + (long long)i * nthr;
+        if (pi < end) out[pi] = scale * pp.energy(i);
+      }
+      return true;
+    };
+    constexpr int P2 = P >= 4 ? P / 2 : P, P4 = P >= 8 ? P / 4 : P2;
+    const bool done = it.w <= P4 * nthr   ? run(PosePairs<P4>{})
+                      : it.w <= P2 * nthr ? run(PosePairs<P2>{})
+                                          : run(PosePairs<P>{});
+    if (!done) return;
     qg += Q;
   }
 }

@@ -92,6 +92,7 @@ static __global__ void __launch_bounds__(256) slice_reduce_kernel(const float *_
 // Poses are processed in pairs (i = 2j, 2j+1) so the distance and accumulate steps use the packed
 // f32x2 instructions; with P == 1 the second lane duplicates the first and is dropped.
 template <int P> struct PosePairs {
+  static constexpr int kP = P;
   static constexpr int NP = (P + 1) / 2;
   float2 e[NP], lx[NP], ly[NP], lz[NP];
 

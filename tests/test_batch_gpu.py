@@ -77,6 +77,35 @@ def test_persistent_equals_per_ligand_unsplit(ctx, batch_and_refs):
     assert np.array_equal(persistent, np.concatenate(per_lig))
 
 
+def test_short_items_run_with_fewer_poses_per_thread(ctx):
+    # An item that fits in P/4 or P/2 poses per thread (a ligand's last pose block) runs with that
+    # many.  Pose counts around each boundary (P = 16, 64 threads: 256 / 512 / 1024 poses) give the
+    # same bits as a launch with 2 poses per thread, and match the oracle.
+    import dataclasses
+    base = small_batch(seed=3, n=12, plo=50, phi=3000)
+    counts = [1, 255, 256, 257, 511, 512, 513, 1023, 1024, 1025, 1024 + 256, 2048 + 700]
+    rng = np.random.default_rng(4)
+    poses = []
+    for n in counts:
+        p = np.empty((6, n), np.float32)
+        p[:3] = rng.uniform(0, 2 * np.pi, (3, n))
+        p[3:] = rng.uniform(-3, 3, (3, n))
+        poses.append(p)
+    b = dataclasses.replace(base, poses=poses)
+    ctx.upload_batch(b)
+    ctx.run_batch(launch_cfg(16, 64, 1, 64, 1))
+    got = ctx.download_batch()
+    ctx.run_batch(launch_cfg(2, 64, 1, 64, 1))
+    assert np.array_equal(got, ctx.download_batch())
+    ctx.run_batch(launch_cfg(16, 64, 3, 64, 2, cluster=0))
+    split = ctx.download_batch()
+    ctx.run_batch(launch_cfg(2, 32, 3, 64, 4, cluster=0))
+    assert np.array_equal(split, ctx.download_batch())
+    e32, e64 = oracle_batch(b)
+    assert_parity(got, e32, e64)
+    assert_parity(split, e32, e64)
+
+
 @pytest.mark.parametrize("split,ppwi,wgsize", [(2, 8, 128), (5, 4, 64), (8, 16, 32), (64, 2, 64)])
 def test_split_batch_matches_oracle_and_is_deterministic(ctx, batch_and_refs, split, ppwi, wgsize):
     # Protein slices per item (split 64 leaves some slices empty for the 2672-atom protein): parity
