@@ -240,9 +240,10 @@ typedef struct bude_screen_cfg {
   int32_t chunks;     /* ligand chunks (0 or 1: none): with more, the exact rescoring of chunk j
                        * runs beside the surrogate of chunk j+1 (slower on the 1,024-ligand
                        * screen: the rescoring blocks slow the surrogate more than they hide) */
-  bude_launch_cfg rescore; /* pose shape of the exact rescoring: ppwi, wgsize and unroll (split, tile
-                            * and cluster are ignored: exact's split and tile are used); ppwi 0
-                            * picks the shape from the number of poses rescored per ligand */
+  bude_launch_cfg rescore; /* shape of the exact rescoring: ppwi, wgsize, unroll and tile, the
+                            * records per shared-memory stage (0: exact's; it must divide exact's
+                            * tile); split and cluster are ignored: the protein slices are exact's.
+                            * ppwi 0 picks the shape from the number of poses rescored per ligand */
 } bude_screen_cfg;
 
 /* total_ms: the whole call; surrogate_ms: pose transforms and surrogate scoring (until the last

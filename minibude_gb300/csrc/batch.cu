@@ -168,9 +168,9 @@ static int batch_blocks_per_sm(const bude_launch_cfg &cfg, int *per_sm) {
 }
 
 // Records per protein slice of a split evaluation: ceil(natpro_pad / split) in whole tiles.
-static int batch_slice(const Context &c, const bude_launch_cfg &cfg) {
-  const int per = (c.natpro_pad + cfg.split - 1) / cfg.split;
-  return (per + cfg.tile - 1) / cfg.tile * cfg.tile;
+static int batch_slice(const Context &c, int split, int tile) {
+  const int per = (c.natpro_pad + split - 1) / split;
+  return (per + tile - 1) / tile * tile;
 }
 
 // The context's slice-sum buffer for a split evaluation of the whole batch.  Growing it moves the
@@ -186,8 +186,10 @@ static int reserve_batch_partial(Context &c, const bude_launch_cfg &cfg) {
 // the transforms at `xform` into `energies` (through `partial` and a slice reduction when split).
 static int enqueue_items(Context &c, const bude_launch_cfg &cfg, int grid, const int4 *items, int n_items,
                          const float4 *xform, float *energies, float *partial, long long npose_space,
-                         cudaStream_t st = nullptr) {
+                         cudaStream_t st = nullptr, int slice_tile = 0) {
   if (!st) st = c.stream;
+  if (slice_tile <= 0) slice_tile = cfg.tile;
+  if (slice_tile % cfg.tile) return set_error(BUDE_ERR_ARG, "the stage tile must divide the slice tile");
   if (cfg.split > 1 && !partial) return set_error(BUDE_ERR_STATE, "split batch evaluation without a slice buffer");
   cudaError_t e = cudaMemsetAsync(c.b_counter.ptr, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return cuda_error(e, "batch counter reset");
@@ -203,7 +205,7 @@ static int enqueue_items(Context &c, const bude_launch_cfg &cfg, int grid, const
   a.natpro_pad = c.natpro_pad;
   a.tile = cfg.tile;
   a.split = std::max(cfg.split, 1);
-  a.slice = a.split > 1 ? batch_slice(c, cfg) : c.natpro_pad;
+  a.slice = a.split > 1 ? batch_slice(c, a.split, slice_tile) : c.natpro_pad;
   a.partial = partial;
   a.npose_space = npose_space;
   const size_t smem = batch_smem(cfg);
@@ -279,12 +281,12 @@ static int ensure_graph(Context &c, const bude_launch_cfg &cfg) {
 
 int batch_items_enqueue(Context &c, const bude_launch_cfg &cfg, const int4 *items, int n_items, const float4 *xform,
                         float *energies, float *partial, long long npose_space, cudaStream_t st,
-                        int max_blocks_per_sm) {
+                        int max_blocks_per_sm, int slice_tile) {
   int grid = 0;
   int rc = persistent_grid(c, cfg, &grid);
   if (rc) return rc;
   if (max_blocks_per_sm > 0) grid = std::min(grid, max_blocks_per_sm * std::max(c.num_sms, 1));
-  return enqueue_items(c, cfg, grid, items, n_items, xform, energies, partial, npose_space, st);
+  return enqueue_items(c, cfg, grid, items, n_items, xform, energies, partial, npose_space, st, slice_tile);
 }
 
 int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand) {

@@ -82,10 +82,12 @@ int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand);
 // Batch kernel over `items` (energies of the items' poses from the transforms at `xform`).  With
 // cfg.split > 1 the slice sums go through `partial` (at least cfg.split * npose_space floats) and a
 // per-item slice reduction.  On stream `st` (nullptr: the context's stream); max_blocks_per_sm > 0
-// caps the persistent grid, leaving room on each SM for kernels running beside it.
+// caps the persistent grid, leaving room on each SM for kernels running beside it.  slice_tile > 0
+// cuts the protein slices as a launch with that tile would (cfg.tile, the records per shared-memory
+// stage, must divide it): the slices alone fix a pose's arithmetic.
 int batch_items_enqueue(Context &c, const bude_launch_cfg &cfg, const int4 *items, int n_items, const float4 *xform,
                         float *energies, float *partial, long long npose_space, cudaStream_t st = nullptr,
-                        int max_blocks_per_sm = 0);
+                        int max_blocks_per_sm = 0, int slice_tile = 0);
 void release_surrogate(Context &c);
 void release_streamer(Context &c);
 void release_screen(Context &c);

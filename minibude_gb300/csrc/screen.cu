@@ -399,9 +399,11 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
                           : per_lig >= 128 ? bude_launch_cfg{8, 32, cfg.split, cfg.tile, 4, 0}
                                            : bude_launch_cfg{4, 32, cfg.split, cfg.tile, 2, 0};
   if (sc.rescore.ppwi != 0) {
-    small = bude_launch_cfg{sc.rescore.ppwi, sc.rescore.wgsize, cfg.split, cfg.tile, sc.rescore.unroll, 0};
+    small = bude_launch_cfg{sc.rescore.ppwi, sc.rescore.wgsize, cfg.split, sc.rescore.tile > 0 ? sc.rescore.tile : cfg.tile,
+                            sc.rescore.unroll, 0};
     rc = check_cfg(c, small);
     if (rc) return rc;
+    if (cfg.tile % small.tile) return set_error(BUDE_ERR_ARG, "the rescoring tile must divide the exact tile");
   }
   std::vector<int> chunk_lig(nchunks + 1, nl), chunk_item(nchunks + 1, 0);
   std::vector<int4> items;
@@ -462,7 +464,7 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
     const int n_it = chunk_item[j + 1] - chunk_item[j];
     if (n_it > 0)
       rc = batch_items_enqueue(c, small, s.items.as<int4>() + chunk_item[j], n_it, s.comp_xform.as<float4>(),
-                               s.comp_exact.as<float>(), s.partial.as<float>(), ncomp, rs, overlap ? 2 : 0);
+                               s.comp_exact.as<float>(), s.partial.as<float>(), ncomp, rs, overlap ? 2 : 0, cfg.tile);
   }
   if (overlap) {
     cudaEvent_t joined = ready.empty() ? nullptr : ready[0];

@@ -212,8 +212,9 @@ def test_screen_chunks_give_the_same_answer(built_library):
 
 
 def test_screen_rescoring_shape_does_not_change_the_answer(built_library):
-    # The pose shape of the exact rescoring (poses per thread, threads per block, unroll) is free:
-    # every shape gives the same energies bit for bit; a shape the kernel does not have is refused.
+    # The shape of the exact rescoring (poses per thread, threads per block, unroll, stage size) is
+    # free: every shape gives the same energies bit for bit; a shape the kernel does not have is
+    # refused.
     from minibude_gb300.capi import BudeError, BudeLaunchCfg
     protein, ff = small_protein()
     batch = synthetic_batch(BatchSpec("t", 12, 16, 64, 3000, 9000), protein, ff, 17)
@@ -223,11 +224,14 @@ def test_screen_rescoring_shape_does_not_change_the_answer(built_library):
         ctx.surrogate_init(protein, ff, seed=2)
         ctx.surrogate_train(2, batch_poses=1024, lr=2e-3, seed=3)
         base = None
-        for p, w, u in ((0, 0, 0), (8, 32, 4), (4, 64, 2), (16, 32, 1), (2, 96, 2)):
-            ctx.screen(exact, audit_tol=1e9, seed=5, rescore_cfg=BudeLaunchCfg(p, w, 0, 0, u, 0))
+        # (ppwi, wgsize, unroll, records per shared-memory stage; 0: the exact launch's 64)
+        for p, w, u, t in ((0, 0, 0, 0), (8, 32, 4, 0), (4, 64, 2, 32), (16, 32, 1, 16), (2, 96, 2, 8)):
+            ctx.screen(exact, audit_tol=1e9, seed=5, rescore_cfg=BudeLaunchCfg(p, w, 0, t, u, 0))
             got = ctx.screen_download(batch.nligands)
             if base is None:
                 base = got
-            assert all(np.array_equal(a, b) for a, b in zip(got, base)), (p, w, u)
+            assert all(np.array_equal(a, b) for a, b in zip(got, base)), (p, w, u, t)
         with pytest.raises(BudeError):
             ctx.screen(exact, rescore_cfg=BudeLaunchCfg(3, 32, 0, 0, 1, 0))
+        with pytest.raises(BudeError):  # the stage must divide the exact launch's tile
+            ctx.screen(exact, rescore_cfg=BudeLaunchCfg(8, 32, 0, 48, 1, 0))
