@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <ctime>
 #include <fstream>
 #include <functional>
@@ -35,6 +36,15 @@
 #include <stdexcept>
 #include <string>
 #include <vector>
+
+#if __has_include("meta_build.h")
+#include "meta_build.h" // written by the build: version, compile commands, git state
+#endif
+#ifndef GB300_BUDE_VERSION
+#define GB300_BUDE_VERSION "0.1"
+#define GB300_BUDE_COMPILE_COMMANDS {}
+#define GB300_BUDE_VCS_RETRIEVED_STATE 0
+#endif
 
 namespace {
 
@@ -387,6 +397,59 @@ bool runAll(const Cli &cli) {
   return std::all_of(results.begin(), results.end(), [](const Outcome &r) { return r.valid; });
 }
 
+// The host CPU block of the YAML header (src/main.cpp:588-631 prints it through the cpu_features
+// library): the same keys, read here from /proc/cpuinfo; "~" where it has none of them.
+void print_host_cpu() {
+  std::ifstream in("/proc/cpuinfo");
+  std::map<std::string, std::string> f;
+  for (std::string line; std::getline(in, line);) {
+    const auto colon = line.find(':');
+    if (colon == std::string::npos) {
+      if (!f.empty()) break; // the first processor's block is enough
+      continue;
+    }
+    auto trim = [](std::string x) {
+      const auto a = x.find_first_not_of(" \t"), b = x.find_last_not_of(" \t");
+      return a == std::string::npos ? std::string() : x.substr(a, b - a + 1);
+    };
+    f.emplace(trim(line.substr(0, colon)), trim(line.substr(colon + 1)));
+  }
+  auto num = [&](const char *k) { return std::to_string(std::strtol(f[k].c_str(), nullptr, 0)); };
+  std::cout << "host_cpu:\n";
+  if (f.count("vendor_id")) {
+    std::cout << "  arch:     \"x86 (" << f["vendor_id"] << ")\"\n"
+              << "  brand:    \"" << f["model name"] << "\"\n"
+              << "  family:   \"" << f["cpu family"] << "\"\n"
+              << "  model:    \"" << f["model"] << "\"\n"
+              << "  stepping: \"" << f["stepping"] << "\"" << std::endl;
+  } else if (f.count("CPU implementer")) {
+    std::cout << "  arch:        \"aarch64\"\n"
+              << "  implementer: \"" << num("CPU implementer") << "\"\n"
+              << "  variant:     \"" << num("CPU variant") << "\"\n"
+              << "  part:        \"" << num("CPU part") << "\"\n"
+              << "  revision:    \"" << num("CPU revision") << "\"" << std::endl;
+  } else {
+    std::cout << "  ~" << std::endl;
+  }
+}
+
+// Version, compile commands and git state of this build (src/main.cpp:570-586).
+void print_provenance() {
+  const std::vector<std::string> cmds = GB300_BUDE_COMPILE_COMMANDS;
+  std::cout << "miniBUDE:  gb300 " GB300_BUDE_VERSION " (" << bude_gpu_version() << ")\n"
+            << "compile_commands:\n";
+  for (const std::string &c : cmds) std::cout << "   - \"" << c << "\"\n";
+  std::cout << "vcs:\n";
+#if GB300_BUDE_VCS_RETRIEVED_STATE
+  std::cout << "  commit:  " << GB300_BUDE_VCS_HEAD_SHA1 << (GB300_BUDE_VCS_IS_DIRTY ? "*" : "") << "\n"
+            << "  author:  \"" << GB300_BUDE_VCS_AUTHOR_NAME << " (" << GB300_BUDE_VCS_AUTHOR_EMAIL << ")\"\n"
+            << "  date:    \"" << GB300_BUDE_VCS_COMMIT_DATE_ISO8601 << "\"\n"
+            << "  subject: \"" << GB300_BUDE_VCS_COMMIT_SUBJECT << "\"\n";
+#else
+  std::cout << "   # not built from a git checkout: no commit recorded\n";
+#endif
+}
+
 } // namespace
 
 int main(int argc, char *argv[]) {
@@ -395,11 +458,9 @@ int main(int argc, char *argv[]) {
     const Params &p = cli.params;
     if (!p.csv) {
       const std::time_t t = std::time(nullptr);
-      std::cout << "miniBUDE:  gb300 (" << bude_gpu_version() << ")\n"
-                << "compile_commands:\n   - \"nvcc -gencode arch=compute_103a,code=sm_103a -O3 (libbude_gb300.so)\"\n"
-                << "vcs:\n   # see the repository\n"
-                << "host_cpu:\n  ~\n"
-                << "time: { epoch_s:" << t << ", formatted: \"" << std::put_time(std::gmtime(&t), "%c %Z") << "\" }"
+      print_provenance();
+      print_host_cpu();
+      std::cout << "time: { epoch_s:" << t << ", formatted: \"" << std::put_time(std::gmtime(&t), "%c %Z") << "\" }"
                 << std::endl;
       if (!p.list)
         std::cout << "deck:\n"

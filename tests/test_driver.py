@@ -44,6 +44,21 @@ def test_bad_ppwi_and_ints(driver):
     assert r.returncode != 0 and "no value was given" in r.stderr
 
 
+def test_yaml_header_provenance(driver):
+    # The header the reference prints before any device work (src/main.cpp:570-636): version,
+    # every compile command of this build, the git state it was built from, the host CPU.
+    # `--list` needs a device afterwards, so only the header is checked here.
+    out = run(driver, "--list").stdout
+    head = out[:out.index("time: {")]
+    assert head.startswith("miniBUDE:  gb300 ")
+    cmds = re.findall(r'^   - "(.*)"$', head, re.M)
+    assert len(cmds) >= 10 and sum("arch=compute_103a,code=sm_103a" in c for c in cmds) >= 9
+    vcs = head[head.index("vcs:"):head.index("host_cpu:")]
+    assert re.search(r"commit:  [0-9a-f]{40}\*?\n", vcs) or "# not built from a git checkout" in vcs
+    cpu = head[head.index("host_cpu:"):]
+    assert re.search(r'arch: +"(x86 \(|aarch64)', cpu) or cpu.strip().endswith("~")
+
+
 def test_deck_errors(driver, tmp_path):
     r = run(driver, "--deck", os.path.join(GOLDEN, "bm1_head"), "-n", "5000")
     assert r.returncode != 0 and "exceeded max poses" in r.stderr
@@ -76,10 +91,19 @@ def test_bm1_head_yaml(driver, tmp_path):
 def test_csv_and_list(driver):
     r = run(driver, "--list")
     assert r.returncode == 0 and "GB300" in r.stdout
-    r = run(driver, "--deck", os.path.join(GOLDEN, "small_head"), "-p", "4", "-w", "128", "--csv")
+    r = run(driver, "--deck", os.path.join(GOLDEN, "small_head"), "-p", "4,8", "-w", "64,128", "--csv")
     assert r.returncode == 0
     rows = [l for l in r.stdout.splitlines() if not l.startswith("#")]
-    assert rows[0].startswith("ppwi,wgsize,sum_ms") and rows[1].startswith("4,128,")
+    assert rows[0].startswith("ppwi,wgsize,sum_ms") and rows[1].startswith("4,64,")
+    # The reference's heatmap.py reads this output as pandas.read_csv(comment="#", skiprows=1)
+    # and pivots sum_ms over (ppwi, wgsize): the same read, without pandas.
+    lines = [l.split("#")[0] for l in r.stdout.splitlines()[1:]]
+    lines = [l for l in lines if l.strip()]
+    head = lines[0].split(",")
+    table = np.array([[float(x) for x in l.split(",")] for l in lines[1:]])
+    cols = {k: table[:, head.index(k)] for k in ("ppwi", "wgsize", "sum_ms")}
+    assert sorted(set(cols["ppwi"])) == [4, 8] and sorted(set(cols["wgsize"])) == [64, 128]
+    assert len(table) == 4 and np.all(cols["sum_ms"] > 0)
 
 
 @pytest.mark.gpu
