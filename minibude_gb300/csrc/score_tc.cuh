@@ -12,8 +12,10 @@
 //      signalled through the group's mbarrier;
 //   3. after each layer loads its row of D (= z) from TMEM, applies the activation (mlp.cuh:
 //      act_pair, FMA pipe only) and writes the BF16 row back into `act` as the next layer's input;
-//   4. runs the output layer as one more UMMA with N = 16: D[:, 0] + D[:, 1] = h3 . w4, with w4
-//      split into two BF16 parts (rows 0 and 1 of the B tile), and adds it to the pose's energy.
+//   4. computes the output layer on the FMA pipe from the layer-3 accumulators: h3 (rounded to
+//      BF16, the operand a fourth UMMA would read) . w4 in FP32, added to the pose's energy.  (An
+//      N = 16 UMMA for it spent a fifth of the tensor time on 1% of the FLOPs and a fourth UMMA
+//      round trip per atom; measured 251 M poses/s with it, 257 M without.)
 // The bias enters as a K = 16 UMMA of a tile of ones against b_l split into three BF16 parts
 // (k = 0, 1, 2), so no FP32 add is left in the epilogue.  The groups of a block share the weights in
 // shared memory and interleave, so one group's epilogue overlaps another's MMAs.  Every mbarrier
@@ -31,7 +33,6 @@ constexpr int kTcGroups = 4;         // tile groups per block when the scorer ru
 constexpr int kTcGroupThreads = 128; // warp w of a group reads TMEM lanes 32w .. 32w + 31
 constexpr int kTcCols = 128;         // TMEM columns per group
 constexpr int kTcBiasK = 16;         // K of the bias UMMA (3 of 16 used)
-constexpr int kTcOutN = 16;          // N of the output UMMA (2 of 16 used)
 
 template <int G> struct TcSmem {
   alignas(128) unsigned char w1[kHid * kFeat * 2];          // W1: [128 out][32 in], K-major
@@ -39,16 +40,16 @@ template <int G> struct TcSmem {
   alignas(128) unsigned char w3[kHid * kHid * 2];           // W3
   alignas(128) unsigned char bias[3][kHid * kTcBiasK * 2];  // b_l in three BF16 parts at k = 0..2
   alignas(128) unsigned char ones[kHid * kTcBiasK * 2];     // 1 at k = 0..2
-  alignas(128) unsigned char w4[kTcOutN * kHid * 2];        // w4 in two BF16 parts at n = 0, 1
   alignas(128) unsigned char act[G][kHid * kHid * 2];         // per group: the layer input tile
+  alignas(16) float w4f[kHid];                               // output weights, FP32
   uint4 emb[kMaxTypes * 2];                                  // type embeddings (16 BF16 each)
   alignas(8) uint64_t bar[G];
   uint32_t tmem;
 };
 
-static_assert(offsetof(TcSmem<4>, w4) + sizeof(TcSmem<4>::w4) - offsetof(TcSmem<4>, bias) ==
-                  sizeof(TcSmem<4>::bias) + sizeof(TcSmem<4>::ones) + sizeof(TcSmem<4>::w4),
-              "bias, ones and w4 tiles are contiguous (zeroed as one range)");
+static_assert(offsetof(TcSmem<4>, ones) + sizeof(TcSmem<4>::ones) - offsetof(TcSmem<4>, bias) ==
+                  sizeof(TcSmem<4>::bias) + sizeof(TcSmem<4>::ones),
+              "bias and ones tiles are contiguous (zeroed as one range)");
 static_assert(sizeof(TcSmem<4>) <= 227 * 1024, "one block per SM fits the 227 KB shared-memory limit");
 // Every variant keeps a second scorer block (and its TMEM allocation) off an SM.
 static_assert(sizeof(TcSmem<3>) > 114 * 1024, "shared memory keeps a second scorer block off the SM");
@@ -74,18 +75,19 @@ __device__ __forceinline__ void to_kmajor(unsigned char *dst, const __nv_bfloat1
   }
 }
 
-// The block's constant tiles: weights, bias and output tiles, the ones tile, embeddings.
+// The block's constant tiles: weights, bias tiles, the ones tile, output weights, embeddings.
 template <class Smem> __device__ __forceinline__ void tc_setup(Smem &s, const MlpWeights &W) {
   const int tid = threadIdx.x;
   {
     uint4 *z = reinterpret_cast<uint4 *>(s.bias);
-    const int n16 = (int)((sizeof s.bias + sizeof s.ones + sizeof s.w4) / 16);
+    const int n16 = (int)((sizeof s.bias + sizeof s.ones) / 16);
     for (int i = tid; i < n16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
   }
   to_kmajor(s.w1, W.w1, kHid, kFeat);
   to_kmajor(s.w2, W.w2, kHid, kHid);
   to_kmajor(s.w3, W.w3, kHid, kHid);
   for (int i = tid; i < kMaxTypes * 2; i += blockDim.x) s.emb[i] = __ldg(reinterpret_cast<const uint4 *>(W.emb) + i);
+  for (int i = tid; i < kHid; i += blockDim.x) s.w4f[i] = __ldg(&W.w4[i]);
   __syncthreads(); // zeroed tiles before their non-zero entries
   for (int i = tid; i < 3 * kHid; i += blockDim.x) {
     const int l = i / kHid, n = i % kHid;
@@ -99,12 +101,6 @@ template <class Smem> __device__ __forceinline__ void tc_setup(Smem &s, const Ml
   }
   for (int m = tid; m < kHid; m += blockDim.x)
     for (int k = 0; k < 3; ++k) st_bf16(s.ones, kmajor_offset(m, k, kTcBiasK), 1.f);
-  for (int k = tid; k < kHid; k += blockDim.x) {
-    const float v = __ldg(&W.w4[k]);
-    const float hi = __bfloat162float(__float2bfloat16_rn(v));
-    st_bf16(s.w4, kmajor_offset(0, k, kHid), hi);
-    st_bf16(s.w4, kmajor_offset(1, k, kHid), v - hi);
-  }
 }
 
 template <int G>
@@ -130,7 +126,7 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
   const uint32_t lane_addr = tmem + ((uint32_t)((lt / 32) * 32) << 16);
   unsigned char *act = s.act[g];
   const uint32_t act_a = smem_u32(act), ones_a = smem_u32(s.ones);
-  const uint32_t idesc = umma_idesc_bf16(kHid, kHid), idesc_out = umma_idesc_bf16(kHid, kTcOutN);
+  const uint32_t idesc = umma_idesc_bf16(kHid, kHid);
   const float b4 = __ldg(a.W.b4);
   uint64_t *bar = &s.bar[g];
   uint32_t phase = 0;
@@ -195,24 +191,24 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
       hidden(smem_u32(s.w2), smem_u32(s.bias[1]), kHid);
       epilogue();
       hidden(smem_u32(s.w3), smem_u32(s.bias[2]), kHid);
-      epilogue();
-      // Output layer: h3 . w4 (two BF16 parts) in TMEM columns 0 and 1.
-      if (lt == 0) {
-        tc_fence_after();
-        const uint32_t sbo = (kHid / 8) * 128u;
-        const uint32_t w4a = smem_u32(s.w4);
-        for (int kk = 0; kk < kHid / 16; ++kk)
-          umma_bf16(tmem, umma_desc(act_a + kk * 256u, 128u, sbo), umma_desc(w4a + kk * 256u, 128u, sbo), idesc_out,
-                    kk > 0 ? 1u : 0u);
-        umma_commit(bar);
+      // Output layer on the FMA pipe: h3 (rounded to BF16, as the next UMMA would read it) . w4
+      // straight from the layer-3 accumulators.
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 1
+      for (int c = 0; c < kHid / 32; ++c) {
+        uint32_t v[32];
+        tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
+        tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; i += 2) {
+          const float4 w = *reinterpret_cast<const float4 *>(&s.w4f[c * 32 + 2 * i]);
+          acc = fma2(unpack_bf16(act_pair(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]))),
+                     make_float2(w.x, w.y), acc);
+          acc = fma2(unpack_bf16(act_pair(__uint_as_float(v[2 * i + 2]), __uint_as_float(v[2 * i + 3]))),
+                     make_float2(w.z, w.w), acc);
+        }
       }
-      if (!mbar_wait_bounded(bar, phase)) failed = true;
-      phase ^= 1u;
-      tc_fence_after();
-      uint32_t y[2];
-      tmem_ld2(lane_addr, y);
-      tmem_wait_ld();
-      e += __uint_as_float(y[0]) + __uint_as_float(y[1]);
+      e += acc.x + acc.y;
       tc_fence_before(); // the next atom's barrier orders these TMEM reads before the next UMMA
     }
     // Group-uniform exit: every thread of the group leaves together.
