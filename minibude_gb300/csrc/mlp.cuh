@@ -11,6 +11,8 @@
 #include <cuda_bf16.h>
 #include <cstdint>
 
+#include "ptx.cuh"
+
 namespace bude {
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -56,8 +58,15 @@ __device__ __forceinline__ float act(float z) {
   return z * s;
 }
 
-// Two pre-activations -> packed BF16 activations (lo = z0, hi = z1).
-__device__ __forceinline__ uint32_t act_pair(float z0, float z1) { return pack_bf16(act(z0), act(z1)); }
+// Two pre-activations -> packed BF16 activations (lo = z0, hi = z1): act() on both, the two
+// multiplies as one packed f32x2 instruction (rounded per lane exactly as the scalar form).
+__device__ __forceinline__ uint32_t act_pair(float z0, float z1) {
+  float s0, s1;
+  asm("fma.rn.sat.f32 %0, %1, %2, 0f3F000000;" : "=f"(s0) : "f"(z0), "f"(kActSlope));
+  asm("fma.rn.sat.f32 %0, %1, %2, 0f3F000000;" : "=f"(s1) : "f"(z1), "f"(kActSlope));
+  const float2 h = mul2(make_float2(z0, z1), make_float2(s0, s1));
+  return pack_bf16(h.x, h.y);
+}
 
 // dh/dz: 0 below -3, 1 above 3, z / 3 + 1/2 between.
 __device__ __forceinline__ float act_grad(float z) {
