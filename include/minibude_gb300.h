@@ -273,6 +273,13 @@ int bude_screen_download(bude_gpu_ctx *ctx, float *final_energies, uint8_t *resc
  * and exact kernels count one each). */
 int bude_gpu_launch_count(const bude_gpu_ctx *ctx, int64_t *count);
 
+/* Self-test of the failure path (no counterpart in the reference): runs one kernel that waits on
+ * an mbarrier nothing arrives on, bounded to limit_us microseconds (1..1e6), exactly as every
+ * device wait of the library is bounded.  Returns BUDE_ERR_TIMEOUT with the error text of a real
+ * timeout, clears the error word, and leaves the context usable.  elapsed_ms (optional) receives
+ * the kernel's time. */
+int bude_gpu_selftest_wait(bude_gpu_ctx *ctx, int32_t limit_us, float *elapsed_ms);
+
 /* One exact evaluation that allocates no device memory.  This entry point has no counterpart in
  * the reference.  It is for callers that may not allocate GPU memory themselves: code running
  * inside another framework whose allocator owns the device heap, plugin hosts that hand a plugin

@@ -114,6 +114,7 @@ SIGNATURES = [
     ("bude_screen_run", ctypes.c_int, [_P, ctypes.POINTER(BudeScreenCfg), ctypes.POINTER(BudeScreenStats)]),
     ("bude_screen_download", ctypes.c_int, [_P, c_float_p, _P, c_float_p, c_int64]),
     ("bude_gpu_launch_count", ctypes.c_int, [_P, ctypes.POINTER(c_int64)]),
+    ("bude_gpu_selftest_wait", ctypes.c_int, [_P, c_int32, ctypes.POINTER(ctypes.c_float)]),
     ("bude_gpu_fasten_noalloc", ctypes.c_int, [_P, c_int32, _P, c_int32, _P, c_int32, _P, c_int64, c_int64, _P, _P]),
     ("bude_host_alloc", ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
     ("bude_host_free", ctypes.c_int, [c_void_p]),

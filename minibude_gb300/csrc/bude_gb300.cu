@@ -241,6 +241,19 @@ int launch_exact_range(Context &c, const bude_launch_cfg &cfg, const float4 *lig
   return BUDE_OK;
 }
 
+// Self-test of the bounded wait: one thread waits on an mbarrier that nothing arrives on, with a
+// limit of limit_ns, and sets bit 0 of the error word when the wait runs out -- the path every
+// kernel of the library takes when one of its waits gives up.
+static __global__ void wait_selftest_kernel(unsigned int *err, unsigned long long limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+    if (!mbar_wait_bounded(&bar, 0, limit_ns)) atomicOr(err, 1u);
+    mbar_inval(&bar);
+  }
+}
+
 // Read (and clear) the device error word after the stream has drained.
 int check_device_error(Context &c) {
   unsigned int h = 0;
@@ -574,6 +587,26 @@ int bude_gpu_fasten(int device, int32_t ppwi, int32_t wgsize, const bude_atom *p
   bude_gpu_destroy(ctx);
   if (rc) bude::set_error(rc, "%s", keep.c_str());
   return rc;
+}
+
+int bude_gpu_selftest_wait(bude_gpu_ctx *ctx, int32_t limit_us, float *elapsed_ms) {
+  if (!ctx) return set_error(BUDE_ERR_ARG, "NULL context");
+  if (limit_us < 1 || limit_us > 1000000) return set_error(BUDE_ERR_ARG, "limit_us must be in [1, 1000000]");
+  bude::Context &c = *ctx;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c.stream);
+  bude::wait_selftest_kernel<<<1, 32, 0, c.stream>>>(c.err.as<unsigned>(), 1000ull * (unsigned long long)limit_us);
+  cudaError_t e = cudaGetLastError();
+  cudaEventRecord(e1, c.stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  if (e == cudaSuccess && elapsed_ms) cudaEventElapsedTime(elapsed_ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return cuda_error(e, "wait_selftest_kernel");
+  c.launches++;
+  return bude::check_device_error(c);
 }
 
 int bude_gpu_launch_count(const bude_gpu_ctx *ctx, int64_t *count) {

@@ -62,6 +62,11 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                : "memory");
 }
 
+// Retire a barrier before its shared memory is left (used where a wait gave up on it).
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // One bounded probe of the barrier's phase; true once the phase with `parity` has completed.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t done;
@@ -87,12 +92,12 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 constexpr uint64_t kWaitLimitNs = 1000ull * 1000ull * 1000ull;
 constexpr uint32_t kWaitMaxProbes = 1u << 26;
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   for (uint32_t it = 1; it < kWaitMaxProbes; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 255u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    if ((it & 255u) == 0 && globaltimer_ns() - t0 > limit_ns) return false;
   }
   return false;
 }

@@ -248,6 +248,11 @@ class GpuContext:
         check(self._lib.bude_screen_download(self.handle, fptr(final), ptr(rescored), fptr(err), self.batch_poses))
         return final, rescored.astype(bool), err[:nligands]
 
+    def selftest_wait(self, limit_us: int) -> Tuple[int, float]:
+        """Run the bounded-wait self-test kernel (bude_gpu_selftest_wait): (status, kernel ms)."""
+        ms = ctypes.c_float()
+        return self._lib.bude_gpu_selftest_wait(self.handle, int(limit_us), ctypes.byref(ms)), ms.value
+
     def launch_count(self) -> int:
         n = ctypes.c_int64()
         check(self._lib.bude_gpu_launch_count(self.handle, ctypes.byref(n)))

@@ -200,3 +200,25 @@ def test_score_host_round_trip(ctx):
     assert_parity(pin_e.array.copy(), refs, f64)
     pin_p.free()
     pin_e.free()
+
+
+def test_bounded_wait_runs_out_and_the_context_stays_usable(built_library):
+    # A device wait that can never finish (an mbarrier nothing arrives on) gives up at its limit,
+    # the host reads BUDE_ERR_TIMEOUT with the error text of a real timeout, and the context goes
+    # on working: the next evaluation matches one from before.
+    from minibude_gb300 import capi
+    from minibude_gb300.capi import BUDE_ERR_TIMEOUT
+    deck, _, _ = load_golden("bm1_head")
+    with GpuContext(0) as ctx:
+        ctx.upload(deck)
+        ctx.run(launch_cfg(8, 128))
+        before = ctx.download()
+        for limit_us in (200, 2000):
+            rc, ms = ctx.selftest_wait(limit_us)
+            assert rc == BUDE_ERR_TIMEOUT
+            assert "bounded device wait ran out" in capi.last_error()
+            assert limit_us * 1e-3 <= ms < limit_us * 1e-3 + 50.0, (limit_us, ms)
+        ctx.run(launch_cfg(8, 128))
+        assert np.array_equal(ctx.download(), before)
+        rc, _ = ctx.selftest_wait(0)
+        assert rc != 0 and rc != BUDE_ERR_TIMEOUT
