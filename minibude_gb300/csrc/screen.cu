@@ -311,18 +311,32 @@ void release_screen(Context &c) {
 
 // Items of ppb poses over pose ranges [first[i], first[i] + count[i]) of ligand lig[i].
 static std::vector<int4> range_items(const Context &c, const std::vector<int> &lig, const std::vector<long long> &first,
-                                     const std::vector<int> &count, int ppb) {
+                                     const std::vector<int> &count, const bude_launch_cfg &shape) {
+  const int ppb = shape.ppwi * shape.wgsize;
   std::vector<int> order(lig.size());
   for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
     return c.lig_off[lig[x] + 1] - c.lig_off[lig[x]] > c.lig_off[lig[y] + 1] - c.lig_off[lig[y]];
   });
+  // The batch kernel runs an item of at most ppb/2 or ppb/4 poses with half or a quarter of the
+  // poses per thread (a quarter from 8 poses per thread up).  A remainder r with
+  // ppb/2 < r <= 3ppb/4 is therefore cut into ppb/2 + the rest, which costs 3/4 of one
+  // full-shape item.
   std::vector<int4> items;
   for (int i : order) {
     const int l = lig[i];
-    for (int p = 0; p < count[i]; p += ppb)
-      items.push_back(make_int4(c.lig_off[l], c.lig_off[l + 1] - c.lig_off[l], (int)(first[i] + p),
-                                std::min(ppb, count[i] - p)));
+    auto item = [&](int p, int n) {
+      items.push_back(make_int4(c.lig_off[l], c.lig_off[l + 1] - c.lig_off[l], (int)(first[i] + p), n));
+    };
+    int p = 0;
+    for (; count[i] - p >= ppb; p += ppb) item(p, ppb);
+    const int r = count[i] - p;
+    if (shape.ppwi >= 8 && 2 * r > ppb && 4 * r <= 3 * ppb) {
+      item(p, ppb / 2);
+      item(p + ppb / 2, r - ppb / 2);
+    } else if (r > 0) {
+      item(p, r);
+    }
   }
   return items;
 }
@@ -419,7 +433,7 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
       cnt.push_back(k);
     }
     chunk_item[j] = (int)items.size();
-    const std::vector<int4> its = range_items(c, lig, first, cnt, small.ppwi * small.wgsize);
+    const std::vector<int4> its = range_items(c, lig, first, cnt, small);
     items.insert(items.end(), its.begin(), its.end());
   }
   if (nchunks > 0) chunk_item[nchunks] = (int)items.size();
@@ -495,7 +509,7 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
       fb_first.push_back(c.pose_off[l]);
       fb_cnt.push_back((int)(c.pose_off[l + 1] - c.pose_off[l]));
     }
-  rc = run_items(c, s, cfg, range_items(c, fb_lig, fb_first, fb_cnt, cfg.ppwi * cfg.wgsize), c.b_xform.as<float4>(),
+  rc = run_items(c, s, cfg, range_items(c, fb_lig, fb_first, fb_cnt, cfg), c.b_xform.as<float4>(),
                  c.b_energies.as<float>(), np);
   if (rc) return rc;
   cudaEventRecord(ev[3], c.stream);
