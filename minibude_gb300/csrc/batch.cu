@@ -29,6 +29,7 @@ void release_batch(Context &c) {
   c.b_partial.release();
   c.have_batch = false;
   c.items_ppb = 0;
+  c.items_ppwi = 0;
   c.n_items = 0;
 }
 
@@ -87,14 +88,17 @@ int upload_batch(Context &c, const bude_atom *protein, int natpro, const bude_ff
   c.pose_off.assign(pose_off, pose_off + nligands + 1);
   c.batch_poses = total_poses;
   c.items_ppb = 0;
+  c.items_ppwi = 0;
   c.batch_tuned_key = -1;
   c.have_batch = true;
   return BUDE_OK;
 }
 
-// Items of P*W poses, longest (most ligand atoms) first; uploaded when the block size changes.
-static int build_items(Context &c, int ppb, std::vector<int4> *keep = nullptr) {
-  if (c.items_ppb == ppb && !keep) return BUDE_OK;
+// Items of at most P*W poses (for_each_item), longest (most ligand atoms) first; uploaded when the
+// launch shape changes.
+static int build_items(Context &c, int ppwi, int wgsize, std::vector<int4> *keep = nullptr) {
+  const int ppb = ppwi * wgsize;
+  if (c.items_ppb == ppb && c.items_ppwi == ppwi && !keep) return BUDE_OK;
   std::vector<int> order(c.nligands);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
@@ -103,10 +107,9 @@ static int build_items(Context &c, int ppb, std::vector<int4> *keep = nullptr) {
   std::vector<int4> items;
   for (int l : order) {
     const int natlig = c.lig_off[l + 1] - c.lig_off[l];
-    for (long long p = c.pose_off[l]; p < c.pose_off[l + 1]; p += ppb) {
-      const long long n = std::min<long long>(ppb, c.pose_off[l + 1] - p);
-      items.push_back(make_int4(c.lig_off[l], natlig, (int)p, (int)n));
-    }
+    for_each_item(c.pose_off[l + 1] - c.pose_off[l], ppwi, ppb, [&](long long p, int n) {
+      items.push_back(make_int4(c.lig_off[l], natlig, (int)(c.pose_off[l] + p), n));
+    });
   }
   if (c.batch_poses > 0x7fffffffLL) return set_error(BUDE_ERR_ARG, "batch too large for 32-bit pose indices");
   if (keep) {
@@ -121,6 +124,7 @@ static int build_items(Context &c, int ppb, std::vector<int4> *keep = nullptr) {
   }
   c.n_items = (int)items.size();
   c.items_ppb = ppb;
+  c.items_ppwi = ppwi;
   return BUDE_OK;
 }
 
@@ -254,7 +258,7 @@ static int ensure_graph(Context &c, const bude_launch_cfg &cfg) {
                     c.graph_cfg.split == cfg.split;
   if (same) return BUDE_OK;
   drop_graph(c);
-  rc = build_items(c, cfg.ppwi * cfg.wgsize);
+  rc = build_items(c, cfg.ppwi, cfg.wgsize);
   int grid = 0;
   if (!rc) rc = persistent_grid(c, cfg, &grid); // also sets the kernel's shared-memory limit
   if (rc) return rc;
@@ -367,7 +371,7 @@ int autotune_batch(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms
     rc = reserve_batch_partial(c, cfg);
     if (rc) break;
     std::vector<int4> items;
-    rc = build_items(c, cfg.ppwi * cfg.wgsize, &items);
+    rc = build_items(c, cfg.ppwi, cfg.wgsize, &items);
     if (rc) break;
     int grid = 0;
     rc = persistent_grid(c, cfg, &grid);

@@ -44,7 +44,8 @@ struct Context {
   long long batch_poses = 0;
   DevBuf b_ligands, b_poses, b_xform, b_energies, b_items, b_counter;
   DevBuf b_partial; // split x batch_poses slice sums of a split batch evaluation (graph-owned)
-  int items_ppb = 0; // poses per item the device item list was built for
+  int items_ppb = 0;  // poses per item the device item list was built for
+  int items_ppwi = 0; // and poses per thread (the cut of a ligand's last block depends on it)
   int n_items = 0;
   cudaGraphExec_t graph = nullptr;
   bude_launch_cfg graph_cfg{};
@@ -79,6 +80,23 @@ int choose_split(const Context &c, bude_launch_cfg &cfg);
 int choose_split_for(int num_sms, int natpro_pad, long long nposes, bude_launch_cfg &cfg);
 void release_batch(Context &c);
 int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand);
+// Cut a ligand's n poses into batch-kernel items of at most ppb = ppwi * wgsize poses: full blocks,
+// then the remainder r.  The batch kernel runs an item of at most ppb/2 or ppb/4 poses with half or
+// a quarter of the poses per thread (a quarter from 8 poses per thread up), so with ppwi >= 8 a
+// remainder ppb/2 < r <= 3ppb/4 is cut into ppb/2 + the rest: 3/4 of a full item's work.
+// f(first pose offset within the ligand, pose count) is called per item, in pose order.
+template <class F> inline void for_each_item(long long n, int ppwi, int ppb, F &&f) {
+  long long p = 0;
+  for (; n - p >= ppb; p += ppb) f(p, ppb);
+  const int r = (int)(n - p);
+  if (ppwi >= 8 && 2 * r > ppb && 4 * r <= 3 * ppb) {
+    f(p, ppb / 2);
+    f(p + ppb / 2, r - ppb / 2);
+  } else if (r > 0) {
+    f(p, r);
+  }
+}
+
 // Batch kernel over `items` (energies of the items' poses from the transforms at `xform`).  With
 // cfg.split > 1 the slice sums go through `partial` (at least cfg.split * npose_space floats) and a
 // per-item slice reduction.  On stream `st` (nullptr: the context's stream); max_blocks_per_sm > 0

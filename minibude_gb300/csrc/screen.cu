@@ -318,25 +318,12 @@ static std::vector<int4> range_items(const Context &c, const std::vector<int> &l
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
     return c.lig_off[lig[x] + 1] - c.lig_off[lig[x]] > c.lig_off[lig[y] + 1] - c.lig_off[lig[y]];
   });
-  // The batch kernel runs an item of at most ppb/2 or ppb/4 poses with half or a quarter of the
-  // poses per thread (a quarter from 8 poses per thread up).  A remainder r with
-  // ppb/2 < r <= 3ppb/4 is therefore cut into ppb/2 + the rest, which costs 3/4 of one
-  // full-shape item.
   std::vector<int4> items;
   for (int i : order) {
     const int l = lig[i];
-    auto item = [&](int p, int n) {
+    for_each_item(count[i], shape.ppwi, ppb, [&](long long p, int n) {
       items.push_back(make_int4(c.lig_off[l], c.lig_off[l + 1] - c.lig_off[l], (int)(first[i] + p), n));
-    };
-    int p = 0;
-    for (; count[i] - p >= ppb; p += ppb) item(p, ppb);
-    const int r = count[i] - p;
-    if (shape.ppwi >= 8 && 2 * r > ppb && 4 * r <= 3 * ppb) {
-      item(p, ppb / 2);
-      item(p + ppb / 2, r - ppb / 2);
-    } else if (r > 0) {
-      item(p, r);
-    }
+    });
   }
   return items;
 }
