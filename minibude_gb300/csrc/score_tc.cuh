@@ -5,8 +5,10 @@
 // runs beside it).  A group scores one item at a
 // time: up to 128 poses of one ligand, pose r = thread r = TMEM lane r of the group's 128 TMEM
 // columns.  For every ligand atom the group
-//   1. builds each pose's 32 features (surrogate_kernels.cuh: features_of; the field channels
-//      come from the texture unit) into its `act` tile, in the K-major core-matrix layout (tc.cuh);
+//   1. builds each pose's 32 features (the type embedding, and surrogate_kernels.cuh:
+//      field_features, whose field channels come from the texture unit) into its `act` tile, in
+//      the K-major core-matrix layout (tc.cuh); the field features of the next atom are fetched
+//      while this atom's layer-3 UMMA runs;
 //   2. runs layers 1..3 as UMMAs issued by the group's first thread: D[128 x 128] = 1 * B_l^T
 //      (the bias) + act * W_l^T over K = 32, 128, 128, FP32 accumulators in TMEM, completion
 //      signalled through the group's mbarrier;
@@ -132,8 +134,9 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
   uint32_t phase = 0;
   bool failed = false;
 
-  // Hidden layer: D = ones * bias^T + act * W^T over kdim, issued by the group's first thread.
-  auto hidden = [&](uint32_t w, uint32_t bias, int kdim) {
+  // Hidden layer: D = ones * bias^T + act * W^T over kdim, issued by the group's first thread;
+  // layer_wait waits for it.
+  auto layer_issue = [&](uint32_t w, uint32_t bias, int kdim) {
     if (lt == 0) {
       tc_fence_after();
       const uint32_t sbo = (uint32_t)(kdim / 8) * 128u, bsbo = (kTcBiasK / 8) * 128u;
@@ -142,9 +145,15 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
         umma_bf16(tmem, umma_desc(act_a + kk * 256u, 128u, sbo), umma_desc(w + kk * 256u, 128u, sbo), idesc, 1u);
       umma_commit(bar);
     }
+  };
+  auto layer_wait = [&]() {
     if (!mbar_wait_bounded(bar, phase)) failed = true;
     phase ^= 1u;
     tc_fence_after();
+  };
+  auto hidden = [&](uint32_t w, uint32_t bias, int kdim) {
+    layer_issue(w, bias, kdim);
+    layer_wait();
   };
   // Activation of the group's D rows into act (K = 128 layout), then the group barrier.
   auto epilogue = [&]() {
@@ -171,15 +180,22 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
     const float4 *xf = a.xform + (long long)(it.z + min(lt, it.w - 1)) * 3;
     const float4 r0 = __ldg(xf), r1 = __ldg(xf + 1), r2 = __ldg(xf + 2);
     float e = 0.f;
-    for (int il = 0; il < it.y; ++il) {
+    // Type and field features of the atom the next tile scores.  For every atom after the first
+    // they are fetched while the previous atom's layer-3 UMMA runs, so the texture latency is off
+    // the chain's critical path.
+    int tn = 0;
+    uint32_t fp[8];
+    auto fetch = [&](int il) {
       const float4 la = __ldg(&a.ligands[it.x + il]);
-      const int t = __float_as_int(la.w);
-      uint32_t f[kFeat / 2];
-      features_of(a.g, la, r0, r1, r2, s.emb[2 * t], s.emb[2 * t + 1], f);
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, q * 8, kFeat)) =
-            make_uint4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+      tn = __float_as_int(la.w);
+      field_features(a.g, la, r0, r1, r2, fp);
+    };
+    if (it.y > 0) fetch(0);
+    for (int il = 0; il < it.y; ++il) {
+      *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, 0, kFeat)) = s.emb[2 * tn];
+      *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, 8, kFeat)) = s.emb[2 * tn + 1];
+      *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, 16, kFeat)) = make_uint4(fp[0], fp[1], fp[2], fp[3]);
+      *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, 24, kFeat)) = make_uint4(fp[4], fp[5], fp[6], fp[7]);
       fence_proxy_async();
       tc_fence_before();
       if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
@@ -190,7 +206,14 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
       epilogue();
       hidden(smem_u32(s.w2), smem_u32(s.bias[1]), kHid);
       epilogue();
-      hidden(smem_u32(s.w3), smem_u32(s.bias[2]), kHid);
+      layer_issue(smem_u32(s.w3), smem_u32(s.bias[2]), kHid);
+      if (il + 1 < it.y) {
+        fetch(il + 1);
+        // The fetched values are complete before the wait below (no reordering past it).
+        asm volatile("" ::"r"(fp[0]), "r"(fp[1]), "r"(fp[2]), "r"(fp[3]), "r"(fp[4]), "r"(fp[5]), "r"(fp[6]),
+                     "r"(fp[7]), "r"(tn));
+      }
+      layer_wait();
       // Output layer on the FMA pipe: h3 (rounded to BF16, as the next UMMA would read it) . w4
       // straight from the layer-3 accumulators.
       float2 acc = make_float2(0.f, 0.f);

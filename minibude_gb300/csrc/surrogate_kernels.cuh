@@ -151,25 +151,36 @@ __device__ __forceinline__ void sample_field(const FieldGrid &g, float x, float 
   c[12] = tex3D<float>(g.tex[3], u, v, w);
 }
 
-// Features of one (pose, ligand atom) as 16 packed BF16 pairs, from the atom {x, y, z, type bits},
-// the pose's transform rows r0..r2 ({R row, t}) and the type's embedding e0, e1 (16 BF16).
-__device__ __forceinline__ void features_of(const FieldGrid &g, float4 la, float4 r0, float4 r1, float4 r2, uint4 e0,
-                                            uint4 e1, uint32_t (&f)[kFeat / 2]) {
+// Features 16..31 of one (pose, ligand atom) -- the transformed position x 0.1 and the 13 field
+// channels -- as 8 packed BF16 pairs, from the atom {x, y, z, type bits} and the pose's transform
+// rows r0..r2 ({R row, t}).
+__device__ __forceinline__ void field_features(const FieldGrid &g, float4 la, float4 r0, float4 r1, float4 r2,
+                                               uint32_t (&p)[8]) {
   const float x = r0.w + la.x * r0.x + la.y * r0.y + la.z * r0.z;
   const float y = r1.w + la.x * r1.x + la.y * r1.y + la.z * r1.z;
   const float z = r2.w + la.x * r2.x + la.y * r2.y + la.z * r2.z;
-  f[0] = e0.x; f[1] = e0.y; f[2] = e0.z; f[3] = e0.w;
-  f[4] = e1.x; f[5] = e1.y; f[6] = e1.z; f[7] = e1.w;
   float c[kGridCh];
   sample_field(g, x, y, z, c);
-  f[8] = pack_bf16(x * g.xyz_scale, y * g.xyz_scale);
-  f[9] = pack_bf16(z * g.xyz_scale, c[0]);
-  f[10] = pack_bf16(c[1], c[2]);
-  f[11] = pack_bf16(c[3], c[4]);
-  f[12] = pack_bf16(c[5], c[6]);
-  f[13] = pack_bf16(c[7], c[8]);
-  f[14] = pack_bf16(c[9], c[10]);
-  f[15] = pack_bf16(c[11], c[12]);
+  p[0] = pack_bf16(x * g.xyz_scale, y * g.xyz_scale);
+  p[1] = pack_bf16(z * g.xyz_scale, c[0]);
+  p[2] = pack_bf16(c[1], c[2]);
+  p[3] = pack_bf16(c[3], c[4]);
+  p[4] = pack_bf16(c[5], c[6]);
+  p[5] = pack_bf16(c[7], c[8]);
+  p[6] = pack_bf16(c[9], c[10]);
+  p[7] = pack_bf16(c[11], c[12]);
+}
+
+// Features of one (pose, ligand atom) as 16 packed BF16 pairs: the type's embedding e0, e1
+// (features 0..15, 16 BF16) and field_features.
+__device__ __forceinline__ void features_of(const FieldGrid &g, float4 la, float4 r0, float4 r1, float4 r2, uint4 e0,
+                                            uint4 e1, uint32_t (&f)[kFeat / 2]) {
+  f[0] = e0.x; f[1] = e0.y; f[2] = e0.z; f[3] = e0.w;
+  f[4] = e1.x; f[5] = e1.y; f[6] = e1.z; f[7] = e1.w;
+  uint32_t p[8];
+  field_features(g, la, r0, r1, r2, p);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) f[8 + i] = p[i];
 }
 
 __device__ __forceinline__ void atom_features(const MlpWeights &W, const FieldGrid &g, float4 la, const float4 *xf,
