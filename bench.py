@@ -454,7 +454,7 @@ def run_surrogate(args, dist: Dist):
     held = synthetic_batch(BatchSpec("held-64x65536", 64, 16, 64, 65536, 65536), protein, ff, 200 + dist.rank)
     ctx = GpuContext(dist.local_rank)
     ctx.upload_batch(train)
-    ctx.surrogate_init(protein, ff, extent=11.0, spacing=0.4, seed=1)
+    ctx.surrogate_init(protein, ff, extent=11.0, spacing=1.0, seed=1)
     loss, train_ms = ctx.surrogate_train(args.epochs, batch_poses=8192, lr=3e-3, seed=2)
     ctx.upload_batch(held)
     cfg, _ = ctx.autotune_batch()
@@ -519,7 +519,7 @@ def run_screen(args, dist: Dist):
     peaks = measured_peaks()
     ctx = GpuContext(dist.local_rank)
     ctx.upload_batch(train)
-    ctx.surrogate_init(protein, ff, extent=11.0, spacing=0.4, seed=1)
+    ctx.surrogate_init(protein, ff, extent=11.0, spacing=1.0, seed=1)
     if args.surrogate_ckpt and os.path.exists(args.surrogate_ckpt):
         ctx.surrogate_load(args.surrogate_ckpt)
         loss, train_ms = float("nan"), 0.0
