@@ -58,6 +58,8 @@ def parse_args():
                          "1024 ligands (16-80 atoms) x 16384 poses against the bm2 protein, surrogate-screened vs "
                          "batched exhaustive exact")
     ap.add_argument("--epochs", type=int, default=40, help="surrogate training epochs (surrogate/screen workloads)")
+    ap.add_argument("--grid-spacing", type=float, default=1.0,
+                    help="spacing in A of the surrogate's protein-field grid (surrogate/screen workloads)")
     ap.add_argument("--surrogate-ckpt", default=None,
                     help="screen workload: load the trained surrogate from this file if it exists, else train and "
                          "save it there")
@@ -454,7 +456,7 @@ def run_surrogate(args, dist: Dist):
     held = synthetic_batch(BatchSpec("held-64x65536", 64, 16, 64, 65536, 65536), protein, ff, 200 + dist.rank)
     ctx = GpuContext(dist.local_rank)
     ctx.upload_batch(train)
-    ctx.surrogate_init(protein, ff, extent=11.0, spacing=1.0, seed=1)
+    ctx.surrogate_init(protein, ff, extent=11.0, spacing=args.grid_spacing, seed=1)
     loss, train_ms = ctx.surrogate_train(args.epochs, batch_poses=8192, lr=3e-3, seed=2)
     ctx.upload_batch(held)
     cfg, _ = ctx.autotune_batch()
@@ -492,6 +494,7 @@ def run_surrogate(args, dist: Dist):
            "dtype": "bf16 (fp32 accumulate)", "data": "synthetic ligands/poses (seeded) against the 938-atom protein",
            "config": {"workload": "surrogate-train-512x4096-held-64x65536", "train_poses": train.total_poses,
                       "held_poses": held.total_poses, "epochs": args.epochs, "batch": 8192,
+                      "grid_spacing_A": args.grid_spacing,
                       "train_ms": round(train_ms, 1), "final_loss": round(loss, 3),
                       "rmse": round(float(np.sqrt(np.mean((sur - exact) ** 2))), 3),
                       "exact_std": round(float(exact.std()), 3),
@@ -519,7 +522,7 @@ def run_screen(args, dist: Dist):
     peaks = measured_peaks()
     ctx = GpuContext(dist.local_rank)
     ctx.upload_batch(train)
-    ctx.surrogate_init(protein, ff, extent=11.0, spacing=1.0, seed=1)
+    ctx.surrogate_init(protein, ff, extent=11.0, spacing=args.grid_spacing, seed=1)
     if args.surrogate_ckpt and os.path.exists(args.surrogate_ckpt):
         ctx.surrogate_load(args.surrogate_ckpt)
         loss, train_ms = float("nan"), 0.0
@@ -560,6 +563,7 @@ def run_screen(args, dist: Dist):
            "data": "synthetic ligands/poses (seeded) against the reference's bm2 protein",
            "config": {"workload": "screen-1024x16384", "poses": screen.total_poses, "top_frac": 0.02,
                       "audit_frac": 0.005, "audit_tol": 0.05, "epochs": args.epochs, "train_ms": round(train_ms, 1),
+                      "grid_spacing_A": args.grid_spacing,
                       "exhaustive_exact_ms": round(exhaustive_ms, 3),
                       "exhaustive_exact_poses_per_s": round(screen.total_poses / (exhaustive_ms * 1e-3), 1),
                       "speedup_vs_exhaustive": round(exhaustive_ms / step, 3),
