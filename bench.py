@@ -531,7 +531,9 @@ def run_screen(args, dist: Dist):
         if args.surrogate_ckpt:
             ctx.surrogate_save(args.surrogate_ckpt)
     ctx.upload_batch(screen)
-    cfg, _ = ctx.autotune_batch()
+    # Every candidate shape is timed on this batch (its items are large, so each trial runs most
+    # of the batch): the exhaustive comparison is the best batched exact launch.
+    cfg, _ = ctx.autotune_batch(max_ms=30000)
     # batched exhaustive exact scoring (the comparison, and the truth for recall)
     ctx.run_batch(cfg)
     ex_ms = [ctx.run_batch(cfg) for _ in range(max(2, args.steps // 2))]
