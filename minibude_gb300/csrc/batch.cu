@@ -41,9 +41,14 @@ static void drop_graph(Context &c) {
 int upload_batch(Context &c, const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes, int nligands,
                  const bude_atom *atoms, const int32_t *lig_off, const float *poses, long long pose_stride,
                  const int64_t *pose_off) {
+  // A batch of the same shape as the uploaded one (same ligand sizes and pose counts, same protein
+  // and forcefield) keeps its work items, captured graph and tuned launch shape: only the atoms and
+  // poses are copied.
+  const bool same_shape = c.have_batch && nligands == c.nligands && lig_off && pose_off &&
+                          std::equal(lig_off, lig_off + nligands + 1, c.lig_off.begin()) &&
+                          std::equal(pose_off, pose_off + nligands + 1, c.pose_off.begin());
   c.have_batch = false;
   c.have_deck = false;
-  drop_graph(c);
   if (nligands < 0 || !lig_off || !pose_off || ntypes <= 0 || !ff || natpro < 0 || (natpro > 0 && !protein))
     return set_error(BUDE_ERR_ARG, "bad batch sizes or pointers");
   if (lig_off[0] != 0 || pose_off[0] != 0) return set_error(BUDE_ERR_ARG, "batch offsets must start at 0");
@@ -62,27 +67,28 @@ int upload_batch(Context &c, const bude_atom *protein, int natpro, const bude_ff
     if (atoms[i].type < 0 || atoms[i].type >= ntypes)
       return set_error(BUDE_ERR_TYPE, "ligand atom %d of the batch has type %d outside the forcefield (%d types)", i,
                        atoms[i].type, ntypes);
-  // Protein slab (shared layout with the single-deck path).
-  c.ntypes = ntypes;
-  c.natpro = natpro;
-  c.natpro_pad = std::max((natpro + kAtomAlign - 1) / kAtomAlign * kAtomAlign, kAtomAlign);
-  std::vector<float> slab;
-  build_slab(protein, natpro, ff, ntypes, c.natpro_pad, slab);
-  int rc = c.slab.reserve(slab.size() * sizeof(float), "slab");
+  // Protein slab (shared with the single-deck path; rebuilt only for another protein/forcefield).
+  bool rebuilt = false;
+  int rc = ensure_slab(c, protein, natpro, ff, ntypes, &rebuilt);
+  if (rc) return rc;
+  const bool keep = same_shape && !rebuilt;
+  if (!keep) drop_graph(c);
   const long long np = std::max(total_poses, 1LL);
-  if (!rc) rc = c.b_ligands.reserve((size_t)std::max(total_atoms, 1) * 16, "batch ligands");
+  rc = c.b_ligands.reserve((size_t)std::max(total_atoms, 1) * 16, "batch ligands");
   if (!rc) rc = c.b_poses.reserve((size_t)6 * np * sizeof(float), "batch poses");
   if (!rc) rc = c.b_xform.reserve((size_t)12 * np * sizeof(float), "batch transforms");
   if (!rc) rc = c.b_energies.reserve((size_t)np * sizeof(float), "batch energies");
   if (!rc) rc = c.b_counter.reserve(256, "batch work counter");
   if (rc) return rc;
-  cudaError_t e = cudaMemcpy(c.slab.ptr, slab.data(), slab.size() * sizeof(float), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && total_atoms > 0)
-    e = cudaMemcpy(c.b_ligands.ptr, atoms, (size_t)total_atoms * 16, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaSuccess;
+  if (total_atoms > 0) e = cudaMemcpy(c.b_ligands.ptr, atoms, (size_t)total_atoms * 16, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && total_poses > 0)
     e = cudaMemcpy2D(c.b_poses.ptr, (size_t)total_poses * sizeof(float), poses, (size_t)pose_stride * sizeof(float),
                      (size_t)total_poses * sizeof(float), 6, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_error(e, "batch upload");
+  c.have_batch = true;
+  if (keep) return BUDE_OK;
+  ++c.batch_gen;
   c.nligands = nligands;
   c.lig_off.assign(lig_off, lig_off + nligands + 1);
   c.pose_off.assign(pose_off, pose_off + nligands + 1);
@@ -90,7 +96,6 @@ int upload_batch(Context &c, const bude_atom *protein, int natpro, const bude_ff
   c.items_ppb = 0;
   c.items_ppwi = 0;
   c.batch_tuned_key = -1;
-  c.have_batch = true;
   return BUDE_OK;
 }
 

@@ -55,6 +55,31 @@ void build_slab(const bude_atom *protein, int natpro, const bude_ffparams *ff, i
   }
 }
 
+int ensure_slab(Context &c, const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes, bool *rebuilt) {
+  std::vector<unsigned char> key(2 * sizeof(int) + (size_t)natpro * sizeof(bude_atom) +
+                                 (size_t)ntypes * sizeof(bude_ffparams));
+  std::memcpy(key.data(), &natpro, sizeof(int));
+  std::memcpy(key.data() + sizeof(int), &ntypes, sizeof(int));
+  if (natpro > 0) std::memcpy(key.data() + 2 * sizeof(int), protein, (size_t)natpro * sizeof(bude_atom));
+  std::memcpy(key.data() + 2 * sizeof(int) + (size_t)natpro * sizeof(bude_atom), ff,
+              (size_t)ntypes * sizeof(bude_ffparams));
+  if (rebuilt) *rebuilt = false;
+  if (c.slab.ptr && key == c.slab_key) return BUDE_OK;
+  c.slab_key.clear();
+  c.ntypes = ntypes;
+  c.natpro = natpro;
+  c.natpro_pad = std::max((natpro + kAtomAlign - 1) / kAtomAlign * kAtomAlign, kAtomAlign);
+  std::vector<float> slab;
+  build_slab(protein, natpro, ff, ntypes, c.natpro_pad, slab);
+  int rc = c.slab.reserve(slab.size() * sizeof(float), "slab");
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c.slab.ptr, slab.data(), slab.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_error(e, "slab upload");
+  c.slab_key = std::move(key);
+  if (rebuilt) *rebuilt = true;
+  return BUDE_OK;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Device buffers
 int DevBuf::reserve(size_t nbytes, const char *what) {
@@ -313,22 +338,12 @@ int upload_deck(Context &c, const bude_atom *protein, int natpro, const bude_ato
     if (protein[i].type < 0 || protein[i].type >= ntypes)
       return set_error(BUDE_ERR_TYPE, "protein atom %d has type %d outside the forcefield (%d types)", i,
                        protein[i].type, ntypes);
-  c.ntypes = ntypes;
-  c.natpro = natpro;
-  c.natpro_pad = std::max(round_up(natpro, kAtomAlign), kAtomAlign);
-  std::vector<float> slab;
-  build_slab(protein, natpro, ff, ntypes, c.natpro_pad, slab);
-  int rc = c.slab.reserve(slab.size() * sizeof(float), "slab");
+  int rc = ensure_slab(c, protein, natpro, ff, ntypes);
   if (rc) return rc;
-  cudaError_t e = cudaMemcpyAsync(c.slab.ptr, slab.data(), slab.size() * sizeof(float), cudaMemcpyHostToDevice, c.stream);
-  if (e != cudaSuccess) return cuda_error(e, "slab upload");
-  // The host copy must stay alive until the async copy has read it.
-  e = cudaStreamSynchronize(c.stream);
-  if (e != cudaSuccess) return cuda_error(e, "slab upload");
   rc = upload_ligand(c, ligand, natlig);
   if (!rc) rc = upload_poses(c, poses, stride, nposes);
   if (rc) return rc;
-  e = cudaStreamSynchronize(c.stream);
+  cudaError_t e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return cuda_error(e, "deck upload");
   c.have_deck = true;
   return BUDE_OK;

@@ -49,6 +49,7 @@ struct Context {
   int n_items = 0;
   cudaGraphExec_t graph = nullptr;
   bude_launch_cfg graph_cfg{};
+  long long batch_gen = 0; // bumped whenever the batch's shape (ligand sizes, pose counts) changes
   long long batch_tuned_key = -1;
   bude_launch_cfg batch_tuned{};
   float batch_tuned_ms = 0.f;
@@ -59,6 +60,8 @@ struct Context {
   long long tuned_key[3] = {-1, -1, -1};
   bude_launch_cfg tuned{};
   float tuned_ms = 0.f;
+  // the protein and forcefield the slab on the device was built from (ensure_slab)
+  std::vector<unsigned char> slab_key;
 };
 
 int set_error(int code, const char *fmt, ...);
@@ -67,6 +70,11 @@ const char *last_error();
 
 void build_slab(const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes, int natpro_pad,
                 std::vector<float> &slab);
+// Build and upload the protein slab for (protein, forcefield) unless the device already holds the
+// slab of exactly these records; sets natpro, natpro_pad and ntypes.  *rebuilt (optional) tells
+// whether it was rebuilt.
+int ensure_slab(Context &c, const bude_atom *protein, int natpro, const bude_ffparams *ff, int ntypes,
+                bool *rebuilt = nullptr);
 
 int make_context(int device, Context **out);
 void destroy_context(Context *c);

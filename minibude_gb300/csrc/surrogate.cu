@@ -54,7 +54,7 @@ struct Surrogate {
   // scoring
   DevBuf items, scores;
   std::vector<int> item_lig_off; // nligands + 1: first scoring item of each ligand
-  int items_for = 0;
+  long long items_for = -1; // Context::batch_gen the items were built for
   int n_items = 0;
   int scorer = BUDE_SCORER_TCGEN05;
 };
@@ -621,7 +621,7 @@ int surrogate_prepare(Context &c, bool xform_ready) {
   const long long np = c.batch_poses;
   int rc = s.scores.reserve((size_t)std::max(np, 1LL) * 4, "surrogate scores");
   if (rc) return rc;
-  if (s.items_for != (int)np || (int)s.item_lig_off.size() != c.nligands + 1) {
+  if (s.items_for != c.batch_gen) {
     std::vector<int4> items;
     s.item_lig_off.assign(1, 0);
     for (int l = 0; l < c.nligands; ++l) {
@@ -634,7 +634,7 @@ int surrogate_prepare(Context &c, bool xform_ready) {
     if (rc) return rc;
     if (!items.empty()) cudaMemcpy(s.items.ptr, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice);
     s.n_items = (int)items.size();
-    s.items_for = (int)np;
+    s.items_for = c.batch_gen;
   }
   if (!xform_ready) {
     rc = batch_transforms(c);

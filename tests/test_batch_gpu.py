@@ -162,3 +162,63 @@ def test_batch_errors(ctx):
     ctx.upload(deck)
     with pytest.raises(BudeError):
         ctx.run_batch(launch_cfg(8, 128))
+
+
+def _reshaped(b, seed, poses_shift=0):
+    """A batch of the same ligand sizes with other coordinates; poses_shift moves poses between the
+    first two ligands (same ligand count and total pose count, another shape)."""
+    import dataclasses
+    rng = np.random.default_rng(seed)
+    ligs = []
+    for l in b.ligands:
+        m = l.copy()
+        for k in ("x", "y", "z"):
+            m[k] = m[k] + rng.normal(0, 0.3, len(m)).astype(np.float32)
+        ligs.append(m)
+    poses = [p + rng.normal(0, 0.05, p.shape).astype(np.float32) for p in b.poses]
+    if poses_shift:
+        moved = poses[0][:, :poses_shift]
+        poses[0] = np.ascontiguousarray(poses[0][:, poses_shift:])
+        poses[1] = np.ascontiguousarray(np.concatenate([poses[1], moved], axis=1))
+    return dataclasses.replace(b, ligands=ligs, poses=poses)
+
+
+def test_reupload_of_the_same_shape_and_of_another(ctx):
+    # A batch of the same shape re-uses the uploaded batch's work items and captured graph; one
+    # with the same ligand and pose totals but another split rebuilds them.  Either way the
+    # energies equal those of a fresh context.
+    a = small_batch(seed=5, n=6, plo=300, phi=2000)
+    same = _reshaped(a, 1)
+    other = _reshaped(a, 2, poses_shift=97)
+    cfg = launch_cfg(8, 128, 2, 64, 2, cluster=0)
+    ctx.upload_batch(a)
+    ctx.run_batch(cfg)
+    got = {}
+    for name, b in (("same", same), ("other", other)):
+        ctx.upload_batch(b)
+        ctx.run_batch(cfg)
+        got[name] = ctx.download_batch()
+    with GpuContext(0) as fresh:
+        for name, b in (("same", same), ("other", other)):
+            fresh.upload_batch(b)
+            fresh.run_batch(cfg)
+            assert np.array_equal(got[name], fresh.download_batch()), name
+
+
+def test_surrogate_items_follow_the_batch_shape(ctx):
+    # Surrogate scores after a re-upload with the same totals but another per-ligand split equal
+    # those of a fresh context with the same weights.
+    a = small_batch(seed=8, n=5, plo=300, phi=1500)
+    other = _reshaped(a, 3, poses_shift=129)
+    protein, ff = bm2_protein()
+    ctx.upload_batch(a)
+    ctx.surrogate_init(protein, ff, seed=4)
+    ctx.surrogate_score()
+    ctx.upload_batch(other)
+    ctx.surrogate_score()
+    got = ctx.surrogate_download()
+    with GpuContext(0) as fresh:
+        fresh.upload_batch(other)
+        fresh.surrogate_init(protein, ff, seed=4)
+        fresh.surrogate_score()
+        assert np.array_equal(got, fresh.surrogate_download())
