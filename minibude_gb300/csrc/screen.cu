@@ -309,7 +309,8 @@ void release_screen(Context &c) {
   c.screen = nullptr;
 }
 
-// Items of ppb poses over pose ranges [first[i], first[i] + count[i]) of ligand lig[i].
+// Batch-kernel items (for_each_item) over pose ranges [first[i], first[i] + count[i]) of ligand
+// lig[i], longest ligand first.
 static std::vector<int4> range_items(const Context &c, const std::vector<int> &lig, const std::vector<long long> &first,
                                      const std::vector<int> &count, const bude_launch_cfg &shape) {
   const int ppb = shape.ppwi * shape.wgsize;
@@ -392,7 +393,7 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
   // not mostly empty, with the fallback's protein slices (the pose shape does not change the
   // arithmetic of a pose, the slices do).  One-warp blocks of 8 poses per thread (256-pose
   // items) measured fastest on 410 picks per ligand (8 slices: 27.9 ms against 30.5 for 64
-  // threads x 4 poses); fewer picks per ligand get 128-pose items.
+  // threads x 4 poses, before the short-item cut); fewer picks per ligand get 128-pose items.
   int with_picks = 0;
   for (int l = 0; l < nl; ++l) with_picks += counts[2 * l] + counts[2 * l + 1] > 0;
   const long long per_lig = with_picks ? ncomp / with_picks : 0;
