@@ -177,14 +177,16 @@ int bude_gpu_download_batch(bude_gpu_ctx *ctx, float *energies, int64_t total_po
 /* ---- Learned pre-screen (no counterpart in the reference) --------------------------------
  * A per-protein MLP estimates pose energies: per (pose, ligand atom) features -- a 16-wide
  * learned type embedding, the transformed atom position and 13 protein-field channels sampled
- * from a grid precomputed for the protein -- go through 32 -> 128 -> 128 -> 128 -> 1 with SiLU;
- * the outputs are summed per pose.  BF16 weights on BF16 tensor-core GEMMs with FP32
- * accumulation; FP32 master weights and Adam state. */
+ * from a grid precomputed for the protein -- go through 32 -> 128 -> 128 -> 128 -> 1 with
+ * hard-swish activations (h = z * sat(z/6 + 1/2), the piecewise-polynomial form of SiLU); the
+ * outputs are summed per pose.  BF16 weights on BF16 tensor-core GEMMs with FP32 accumulation;
+ * FP32 master weights and Adam state. */
 #define BUDE_SURROGATE_NPARAMS 38404
 
 /* Create (or reset) the context's surrogate for a protein: builds the field grid over
  * [-extent, extent]^3 with `spacing` (at most 400 points a side) and seeds the weights.  At most
- * 64 forcefield types. */
+ * 64 forcefield types.  A 1.0 A spacing keeps the accuracy of finer grids on the reference's
+ * proteins and samples faster than they do (the grid stays in the texture cache). */
 int bude_surrogate_init(bude_gpu_ctx *ctx, const bude_atom *protein, int32_t natpro, const bude_ffparams *forcefield,
                         int32_t ntypes, float extent, float spacing, uint64_t seed);
 
