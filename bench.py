@@ -57,8 +57,8 @@ def parse_args():
                          "2M poses of 512 ligands (938-atom protein), score 64 held-out ligands x 65536 poses; screen: "
                          "1024 ligands (16-80 atoms) x 16384 poses against the bm2 protein, surrogate-screened vs "
                          "batched exhaustive exact")
-    ap.add_argument("--epochs", type=int, default=40, help="surrogate training epochs (surrogate/screen workloads)")
-    ap.add_argument("--grid-spacing", type=float, default=1.0,
+    ap.add_argument("--epochs", type=int, default=80, help="surrogate training epochs (surrogate/screen workloads)")
+    ap.add_argument("--grid-spacing", type=float, default=1.25,
                     help="spacing in A of the surrogate's protein-field grid (surrogate/screen workloads)")
     ap.add_argument("--surrogate-ckpt", default=None,
                     help="screen workload: load the trained surrogate from this file if it exists, else train and "

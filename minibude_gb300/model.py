@@ -170,7 +170,7 @@ class GpuContext:
         return out
 
     # -- learned pre-screen --------------------------------------------------------------------
-    def surrogate_init(self, protein, forcefield, extent: float = 11.0, spacing: float = 1.0, seed: int = 0):
+    def surrogate_init(self, protein, forcefield, extent: float = 11.0, spacing: float = 1.25, seed: int = 0):
         protein, ff = _atoms(protein), _ff(forcefield)
         check(self._lib.bude_surrogate_init(self.handle, ptr(protein), protein.size, ptr(ff), ff.size, extent, spacing,
                                             seed))
