@@ -80,44 +80,56 @@ __host__ __device__ inline int screen_audit_count(float audit_frac, int n, int k
 }
 
 // Radix select over the 32-bit keys key(i) of the eligible poses i < n (3 passes of 11/11/10 bits):
-// *thr = the need-th smallest key, *ties = how many of the keys equal to it are inside the pick.
+// *thr = the need-th smallest key, *ties = how many of the keys equal to it are inside the pick,
+// *eq = how many eligible keys equal it (so eq == ties: every key equal to *thr is picked).  The
+// bin holding the need-th key is found by a block-wide scan of the histogram.
 template <class Key>
-__device__ void radix_select(int n, int need, Key key, int *hist, uint32_t *s_prefix, uint32_t *s_mask, int *s_need,
-                             uint32_t *thr, int *ties) {
+__device__ void radix_select(int n, int need, Key key, int *hist, int *warp_sums, uint32_t *s_prefix, uint32_t *s_mask,
+                             int *s_need, int *s_eq, uint32_t *thr, int *ties, int *eq) {
   if (threadIdx.x == 0) {
     *s_prefix = 0;
     *s_mask = 0;
     *s_need = need;
+    *s_eq = 0;
   }
   __syncthreads();
   const int shifts[3] = {21, 10, 0};
   const int widths[3] = {11, 11, 10};
   for (int pass = 0; pass < 3 && need > 0; ++pass) {
     const int sh = shifts[pass];
-    const uint32_t bm = (1u << widths[pass]) - 1u;
+    const int nb = 1 << widths[pass];
+    const uint32_t bm = (uint32_t)nb - 1u;
     for (int i = threadIdx.x; i < 2048; i += blockDim.x) hist[i] = 0;
     __syncthreads();
     const uint32_t prefix = *s_prefix, mask = *s_mask;
+    const int left = *s_need; // read before block_scan's barriers; rewritten after them
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       uint32_t k;
       if (key(i, &k) && (k & mask) == prefix) atomicAdd(&hist[(k >> sh) & bm], 1);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int left = *s_need, cum = 0;
-      uint32_t b = 0;
-      for (; b < bm; ++b) {
-        if (cum + hist[b] >= left) break;
-        cum += hist[b];
-      }
+    // Thread t owns bins [t * per, t * per + per); the one whose bins hold the left-th key writes
+    // the next prefix.
+    const int per = (nb + (int)blockDim.x - 1) / (int)blockDim.x;
+    const int b0 = (int)threadIdx.x * per;
+    int mine = 0;
+    for (int j = 0; j < per; ++j)
+      if (b0 + j < nb) mine += hist[b0 + j];
+    int tot = 0;
+    const int before = block_scan(mine, warp_sums, &tot);
+    if (before < left && before + mine >= left) {
+      int cum = before, b = b0;
+      while (cum + hist[b] < left) cum += hist[b++];
       *s_need = left - cum;
-      *s_prefix = prefix | (b << sh);
+      *s_prefix = prefix | ((uint32_t)b << sh);
       *s_mask = mask | (bm << sh);
+      *s_eq = hist[b];
     }
     __syncthreads();
   }
   *thr = *s_prefix;
   *ties = *s_need;
+  *eq = *s_eq;
   __syncthreads();
 }
 
@@ -131,31 +143,37 @@ __global__ void __launch_bounds__(kSelThreads) select_kernel(const float *scores
   __shared__ int hist[2048];
   __shared__ int warp_sums[32];
   __shared__ uint32_t s_prefix, s_mask;
-  __shared__ int s_need;
+  __shared__ int s_need, s_eq;
   const int l = lig0 + blockIdx.x;
   const long long off = pose_off[l];
   const int n = (int)(pose_off[l + 1] - off);
   const int k = screen_top_count(top_frac, n);
   const int ka = screen_audit_count(audit_frac, n, k);
   uint32_t T = 0, Ta = 0;
-  int ties = 0, ties_a = 0;
-  // 1. the picks: keys below T, then the first `ties` keys equal to T in pose order
+  int ties = 0, ties_a = 0, eq = 0, eq_a = 0;
+  // 1. the picks: keys below T, then the first `ties` keys equal to T in pose order (a scan only
+  //    when some key equal to T stays out)
   radix_select(
       n, k,
       [&](int i, uint32_t *key) {
         *key = order_key(scores[off + i]);
         return true;
       },
-      hist, &s_prefix, &s_mask, &s_need, &T, &ties);
-  int tie_base = 0;
-  for (int c0 = 0; c0 < n; c0 += blockDim.x) {
-    const int i = c0 + threadIdx.x;
-    const uint32_t key = i < n ? order_key(scores[off + i]) : 0xffffffffu;
-    const int is_tie = (k > 0 && i < n && key == T) ? 1 : 0;
-    int tot = 0;
-    const int rank = block_scan(is_tie, warp_sums, &tot);
-    if (i < n) flag[off + i] = (k > 0 && (key < T || (is_tie && tie_base + rank < ties))) ? 1 : 0;
-    tie_base += tot;
+      hist, warp_sums, &s_prefix, &s_mask, &s_need, &s_eq, &T, &ties, &eq);
+  if (k == 0 || eq == ties) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      flag[off + i] = (k > 0 && order_key(scores[off + i]) <= T) ? 1 : 0;
+  } else {
+    int tie_base = 0;
+    for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+      const int i = c0 + threadIdx.x;
+      const uint32_t key = i < n ? order_key(scores[off + i]) : 0xffffffffu;
+      const int is_tie = (i < n && key == T) ? 1 : 0;
+      int tot = 0;
+      const int rank = block_scan(is_tie, warp_sums, &tot);
+      if (i < n) flag[off + i] = (key < T || (is_tie && tie_base + rank < ties)) ? 1 : 0;
+      tie_base += tot;
+    }
   }
   __threadfence_block();
   __syncthreads();
@@ -166,17 +184,22 @@ __global__ void __launch_bounds__(kSelThreads) select_kernel(const float *scores
         *key = mix_hash(seed, (uint32_t)(off + i));
         return flag[off + i] == 0;
       },
-      hist, &s_prefix, &s_mask, &s_need, &Ta, &ties_a);
-  tie_base = 0;
-  for (int c0 = 0; c0 < n; c0 += blockDim.x) {
-    const int i = c0 + threadIdx.x;
-    const bool free_pose = i < n && flag[off + i] == 0;
-    const uint32_t h = free_pose ? mix_hash(seed, (uint32_t)(off + i)) : 0xffffffffu;
-    const int is_tie = (ka > 0 && free_pose && h == Ta) ? 1 : 0;
-    int tot = 0;
-    const int rank = block_scan(is_tie, warp_sums, &tot);
-    if (free_pose && ka > 0 && (h < Ta || (is_tie && tie_base + rank < ties_a))) flag[off + i] = 2;
-    tie_base += tot;
+      hist, warp_sums, &s_prefix, &s_mask, &s_need, &s_eq, &Ta, &ties_a, &eq_a);
+  if (ka == 0 || eq_a == ties_a) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      if (ka > 0 && flag[off + i] == 0 && mix_hash(seed, (uint32_t)(off + i)) <= Ta) flag[off + i] = 2;
+  } else {
+    int tie_base = 0;
+    for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+      const int i = c0 + threadIdx.x;
+      const bool free_pose = i < n && flag[off + i] == 0;
+      const uint32_t h = free_pose ? mix_hash(seed, (uint32_t)(off + i)) : 0xffffffffu;
+      const int is_tie = (free_pose && h == Ta) ? 1 : 0;
+      int tot = 0;
+      const int rank = block_scan(is_tie, warp_sums, &tot);
+      if (free_pose && (h < Ta || (is_tie && tie_base + rank < ties_a))) flag[off + i] = 2;
+      tie_base += tot;
+    }
   }
   if (threadIdx.x == 0) {
     counts[2 * l] = k;
