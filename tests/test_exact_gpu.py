@@ -222,3 +222,19 @@ def test_bounded_wait_runs_out_and_the_context_stays_usable(built_library):
         assert np.array_equal(ctx.download(), before)
         rc, _ = ctx.selftest_wait(0)
         assert rc != 0 and rc != BUDE_ERR_TIMEOUT
+
+
+@pytest.mark.parametrize("chunk", [1, 7, 333, 4096])
+def test_stream_in_small_chunks_equals_one_shot(ctx, chunk):
+    # Host-resident poses streamed in chunks (bude_gpu_score_stream), from a row-strided array:
+    # every chunk size gives the one-shot energies bit for bit.
+    deck, _, _ = load_golden("bm1_head")
+    ctx.upload(deck)
+    cfg = launch_cfg(4, 64, 2, 32, 2, cluster=0)
+    ctx.run(cfg)
+    want = ctx.download()
+    wide = np.zeros((6, deck.nposes + 5), np.float32)
+    wide[:, :deck.nposes] = deck.poses
+    e = np.full(deck.nposes, np.nan, np.float32)
+    ctx.score_stream(cfg, wide[:, :deck.nposes], e, chunk=chunk)
+    assert np.array_equal(e, want)
