@@ -235,3 +235,33 @@ def test_screen_rescoring_shape_does_not_change_the_answer(built_library):
             ctx.screen(exact, rescore_cfg=BudeLaunchCfg(3, 32, 0, 0, 1, 0))
         with pytest.raises(BudeError):  # the stage must divide the exact launch's tile
             ctx.screen(exact, rescore_cfg=BudeLaunchCfg(8, 32, 0, 48, 1, 0))
+
+
+def test_screen_ragged_ligands(built_library):
+    # Ligands with 0, 1, 2, 50 and 3,000 poses in one screen: every count picks
+    # ceil(top_frac * n) poses plus the audit, a one-pose ligand is rescored whole, and every
+    # rescored energy is the batch kernel's.
+    import dataclasses
+    protein, ff = small_protein()
+    base = synthetic_batch(BatchSpec("t", 5, 16, 64, 3000, 3000), protein, ff, 21)
+    poses = [base.poses[0][:, :0], base.poses[1][:, :1], base.poses[2][:, :2], base.poses[3][:, :50], base.poses[4]]
+    batch = dataclasses.replace(base, poses=[np.ascontiguousarray(p) for p in poses])
+    exact = launch_cfg(8, 64, 4, 64, 2, cluster=0)
+    with GpuContext(0) as ctx:
+        ctx.upload_batch(batch)
+        ctx.run_batch(exact)
+        full = ctx.download_batch()
+        ctx.surrogate_init(protein, ff, seed=6)
+        st = ctx.screen(exact, top_frac=0.02, audit_frac=0.005, audit_tol=1e9, seed=2)
+        final, rescored, err = ctx.screen_download(batch.nligands)
+    off = batch.pose_offsets()
+    want = 0
+    for l in range(batch.nligands):
+        n = int(off[l + 1] - off[l])
+        k = min(n, int(np.ceil(np.float32(0.02) * np.float32(n))))
+        a = min(n - k, int(np.ceil(np.float32(0.005) * np.float32(n))))
+        assert rescored[off[l]:off[l + 1]].sum() == k + a, l
+        want += k + a
+    assert st["rescored_poses"] == want and rescored[off[1]]
+    assert np.array_equal(final[rescored], full[rescored])
+    assert np.all(np.isfinite(final))
