@@ -164,8 +164,28 @@ class GpuContext:
         check(self._lib.bude_gpu_run_batch(self.handle, ctypes.byref(cfg), int(per_ligand), ctypes.byref(ms)))
         return ms.value
 
-    def download_batch(self) -> np.ndarray:
-        out = np.zeros(self.batch_poses, np.float32)
+    def upload_batch_arrays(self, protein, forcefield, atoms, lig_off, poses, pose_off) -> None:
+        """bude_gpu_upload_batch from prepared arrays: the ligands' atoms concatenated, int32 atom
+        offsets and int64 pose offsets (nligands + 1 each), and poses as a float32 [6][total]
+        array with contiguous rows and any row stride (a PinnedBuffer view, for example)."""
+        protein, ff, atoms = _atoms(protein), _ff(forcefield), _atoms(atoms)
+        lig_off = np.ascontiguousarray(lig_off, np.int32)
+        pose_off = np.ascontiguousarray(pose_off, np.int64)
+        if poses.ndim != 2 or poses.shape[0] != 6 or poses.dtype != np.float32 or poses.strides[1] != 4:
+            raise ValueError("poses must be a float32 [6][n] array with contiguous rows")
+        check(self._lib.bude_gpu_upload_batch(self.handle, ptr(protein), protein.size, ptr(ff), ff.size,
+                                              len(lig_off) - 1, ptr(atoms), ptr(lig_off),
+                                              ctypes.c_void_p(poses.ctypes.data), poses.strides[0] // 4,
+                                              ptr(pose_off)))
+        self.batch_poses = poses.shape[1]
+
+    def download_batch(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Energies of the last batch evaluation, into `out` (a float32 array of the batch's pose
+        count, e.g. a PinnedBuffer's) or a new array."""
+        if out is None:
+            out = np.zeros(self.batch_poses, np.float32)
+        elif out.dtype != np.float32 or out.size < self.batch_poses or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float32 array of the batch's pose count")
         check(self._lib.bude_gpu_download_batch(self.handle, fptr(out), self.batch_poses))
         return out
 

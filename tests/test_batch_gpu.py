@@ -222,3 +222,28 @@ def test_surrogate_items_follow_the_batch_shape(ctx):
         fresh.surrogate_init(protein, ff, seed=4)
         fresh.surrogate_score()
         assert np.array_equal(got, fresh.surrogate_download())
+
+
+def test_upload_from_pinned_arrays(ctx, batch_and_refs):
+    # The array form of the batch upload, from a row-strided pinned buffer, and the download into
+    # pinned memory give the energies of the object form.
+    from minibude_gb300.model import PinnedBuffer
+    b, (e32, e64) = batch_and_refs
+    cfg = launch_cfg(8, 128, 1, 64, 2)
+    ctx.upload_batch(b)
+    ctx.run_batch(cfg)
+    want = ctx.download_batch()
+    block = b.pose_block()
+    n = block.shape[1]
+    pin_p, pin_e = PinnedBuffer((6, n + 3)), PinnedBuffer((n,))
+    try:
+        pin_p.array[:, :n] = block
+        ctx.upload_batch_arrays(b.protein, b.forcefield, b.atoms(), b.ligand_offsets(), pin_p.array[:, :n],
+                                b.pose_offsets())
+        ctx.run_batch(cfg)
+        got = ctx.download_batch(pin_e.array)
+        assert np.array_equal(got, want)
+        assert_parity(np.array(got), e32, e64)
+    finally:
+        pin_p.free()
+        pin_e.free()
