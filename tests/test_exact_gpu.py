@@ -238,3 +238,27 @@ def test_stream_in_small_chunks_equals_one_shot(ctx, chunk):
     e = np.full(deck.nposes, np.nan, np.float32)
     ctx.score_stream(cfg, wide[:, :deck.nposes], e, chunk=chunk)
     assert np.array_equal(e, want)
+
+
+@pytest.mark.parametrize("ntypes,natpro,natlig", [(1, 50, 3), (150, 700, 40), (64, 1, 1)])
+def test_forcefield_and_deck_sizes(ctx, ntypes, natpro, natlig):
+    # A one-type and a 150-type forcefield (the slab holds a row per type), a one-atom protein and
+    # ligand: the reference's check passes with and without a protein split.  Against FP64 the
+    # unsplit launch stays within the bound of test_zy_fp64_error (4x the reference's own FP32
+    # error, at least 2e-4); a split adds the slices' partial sums in another order, which on the
+    # 28,000-term energies of the 150-type deck moves a near-zero energy by up to ~5e-4.
+    from minibude_gb300.deck import DeckSpec
+    spec = DeckSpec(f"t{ntypes}", natpro, 15.0, natlig, ntypes, 777)
+    deck = synthetic_deck(spec, seed=ntypes)
+    want = oracle.fasten_f32(deck)
+    f64 = oracle.fasten_f64(deck)
+    ref_err = (np.abs(want.astype(np.float64) - f64) / np.maximum(np.abs(f64), 1.0)).max()
+    ctx.upload(deck)
+    for cfg, bound in ((launch_cfg(8, 64, 1, 32, 2), max(2e-4, 4 * ref_err)),
+                       (launch_cfg(8, 64, 2, 32, 2, cluster=0), 1e-3)):
+        ctx.run(cfg)
+        got = ctx.download()
+        max_diff, failed = validate(got, want)
+        assert not failed and max_diff < 0.025, (cfg.split, max_diff, failed[:5])
+        err = np.abs(got.astype(np.float64) - f64) / np.maximum(np.abs(f64), 1.0)
+        assert err.max() < bound, (cfg.split, err.max(), bound)
