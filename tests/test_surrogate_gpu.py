@@ -265,3 +265,18 @@ def test_screen_ragged_ligands(built_library):
     assert st["rescored_poses"] == want and rescored[off[1]]
     assert np.array_equal(final[rescored], full[rescored])
     assert np.all(np.isfinite(final))
+
+
+def test_screen_from_c(built_library, tmp_path):
+    # minibude_gb300/examples/screen_example.c drives batch upload, exhaustive scoring, surrogate
+    # training and the screen through the C-ABI alone and checks its own results.
+    import os
+    import subprocess
+    from minibude_gb300 import build
+    exe = tmp_path / "screen_example"
+    subprocess.run(["gcc", "-std=c11", "-Wall", f"-I{build.INCLUDE}",
+                    os.path.join(build.PKG, "examples", "screen_example.c"), f"-L{build.PKG}", "-lbude_gb300",
+                    f"-Wl,-rpath,{build.PKG}", "-lm", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "0 mismatching energies" in r.stdout
