@@ -12,7 +12,7 @@
 //      1 - Spearman(surrogate, exact); a ligand whose error exceeds `audit_tol` is rescored
 //      exhaustively with the exact kernel;
 //   5. final energies: exact where rescored, the surrogate's elsewhere.
-// The exact kernel is the judge throughout: everything the screen reports as an energy of a
+// The exact kernel is the arbiter throughout: everything the screen reports as an energy of a
 // selected pose is an exact energy.
 #include <cuda_runtime.h>
 
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(256) audit_kernel(const long long *comp_off, c
   }
   if (threadIdx.x == 0) {
     if (na < 3) {
-      err[l] = 0.f; // too few audit poses to judge: keep the picks
+      err[l] = 0.f; // too few audit poses to measure the error: keep the picks
     } else {
       const double n = na;
       const double cov = red[4][0] / n - (red[0][0] / n) * (red[1][0] / n);

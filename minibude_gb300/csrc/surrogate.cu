@@ -3,7 +3,7 @@
 // No counterpart in the reference.  A per-protein MLP is trained on exact energies of the
 // context's uploaded batch (computed here with the batched exact kernel) and then scores poses
 // for the screening pipeline (screen.cu), where the exact kernel rescores its picks and remains
-// the judge.  Forward, backward and Adam are hand-written kernels driven from this file; every
+// the arbiter of its error.  Forward, backward and Adam are hand-written kernels driven from this file; every
 // reduction (weight, bias and embedding gradients, the loss) is summed in a fixed order, so a
 // training run is deterministic for a given seed.
 #include <cuda_runtime.h>

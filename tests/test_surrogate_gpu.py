@@ -1,6 +1,6 @@
 """The learned pre-screen: MLP forward and gradients against a plain PyTorch FP32 reference,
-training behaviour, checkpoints, and the screening pipeline's invariants (the exact kernel judges
-every pose it reports)."""
+training behaviour, checkpoints, and the screening pipeline's invariants (the exact kernel computes
+the energy of every pose it reports as rescored)."""
 import numpy as np
 import pytest
 
