@@ -38,7 +38,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 from minibude_gb300 import LARGE, SMALL, synthetic_deck  # noqa: E402
-from minibude_gb300.validate import algorithmic_flops  # noqa: E402
+from minibude_gb300.validate import algorithmic_flops, reference_formula_flops  # noqa: E402
 
 METRIC = "exact GInteractions/s"
 UNIT = "GInteractions/s"
@@ -272,7 +272,10 @@ def run_ours(args, dist: Dist):
                            "no measured FP32 peak exists, so this is the nominal peak at the measured max clock",
             "work": "30 FLOP/interaction + 18/(pose, ligand atom) + 28/pose (src/main.cpp:359)",
             "kernel": "exact_kernel", "kernel_ms": round(exact_s * 1e3, 4),
-            "traffic": traffic_per_launch(deck.nposes)}
+            "traffic": traffic_per_launch(deck.nposes),
+            # the reference's PPWI-dependent count (src/main.cpp:359), for a like-for-like GFLOP/s
+            "gflops_reference_formula": round(
+                reference_formula_flops(deck.nposes, deck.natlig, deck.natpro, cfg.ppwi) / exact_s / 1e9, 1)}
     if clk.get("sm_mhz"):
         roof["frac_at_sampled_clock"] = round(achieved / (sms * 128 * 2 * clk["sm_mhz"] * 1e6 / 1e12), 4)
 
@@ -402,7 +405,10 @@ def run_batch(args, dist: Dist):
                         "frac": round(achieved / peak, 4), "kernel": "batch_kernel",
                         "work": "30 FLOP/interaction + 18/(pose, ligand atom) + 28/pose (src/main.cpp:359)",
                         "peak_source": f"{sms} SMs x 128 x 2 x {sm_max:.0f} MHz (nominal at sm_max_mhz)",
-                        "traffic": traffic_per_launch(batch.total_poses, "batch_kernel")}}
+                        "traffic": traffic_per_launch(batch.total_poses, "batch_kernel"),
+                        "gflops_reference_formula": round(sum(
+                            reference_formula_flops(p.shape[1], len(l), batch.natpro, cfg.ppwi)
+                            for l, p in zip(batch.ligands, batch.poses)) / (step_ms * 1e-3) / 1e9, 1)}}
     if not args.no_e2e:
         # End to end through the C-ABI: every step uploads the batch's atoms and poses from pinned
         # host buffers (the protein is compared on the host and its slab kept), runs the batch and

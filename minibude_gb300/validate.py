@@ -93,6 +93,16 @@ def algorithmic_flops(nposes: int, natlig: int, natpro: int) -> float:
     return 30.0 * nposes * natlig * natpro + 18.0 * nposes * natlig + 28.0 * nposes
 
 
+def reference_formula_flops(nposes: int, natlig: int, natpro: int, ppwi: int) -> float:
+    """The reference's own FLOP count for a launch with `ppwi` poses per work-item (src/main.cpp:359:
+    ops_per_wg = 27 P + natlig (2 + 18 P + natpro (10 + 30 P)) + P, times nposes / P groups).  It
+    counts the per-pair setup once per PPWI group, so it depends on PPWI; the PPWI-independent
+    part is `algorithmic_flops`."""
+    p = float(ppwi)
+    ops_per_wg = 27.0 * p + natlig * (2.0 + 18.0 * p + natpro * (10.0 + 30.0 * p)) + p
+    return ops_per_wg * (nposes / p)
+
+
 @dataclasses.dataclass
 class Result:
     valid: bool

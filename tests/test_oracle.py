@@ -75,3 +75,15 @@ def test_oracle_vs_reference_models():
         assert validate(e, r)[0] < 0.005
     s = oracle.ref_serial_fasten(deck.head(64))
     assert validate(e[:64], s)[0] < 0.005
+
+
+@pytest.mark.parametrize("ppwi", [1, 2, 4, 8, 16, 32, 64, 128])
+def test_flop_counts(ppwi):
+    # The reference's count (src/main.cpp:359) is the PPWI-independent algorithmic count plus the
+    # per-pair setup (10 per interaction, 2 per ligand atom) once per group of PPWI poses.
+    from minibude_gb300.validate import algorithmic_flops, reference_formula_flops
+    n, lig, pro = 65536, 26, 938
+    ref = reference_formula_flops(n, lig, pro, ppwi)
+    setup = (n / ppwi) * (2.0 * lig + 10.0 * lig * pro)
+    assert ref == pytest.approx(algorithmic_flops(n, lig, pro) + setup, rel=1e-12)
+    assert reference_formula_flops(n, lig, pro, 2 * ppwi) < ref
