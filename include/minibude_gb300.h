@@ -267,7 +267,8 @@ typedef struct bude_screen_stats {
 int bude_screen_run(bude_gpu_ctx *ctx, const bude_screen_cfg *cfg, bude_screen_stats *stats);
 
 /* Final energies (exact where rescored, surrogate elsewhere), rescored flags (per pose) and the
- * per-ligand audit errors of the last screen; any output may be NULL. */
+ * per-ligand audit errors of the last screen; any output may be NULL.  BUDE_ERR_STATE when the
+ * last screen failed or a batch was uploaded after it (its result belongs to the earlier batch). */
 int bude_screen_download(bude_gpu_ctx *ctx, float *final_energies, uint8_t *rescored, float *audit_error,
                          int64_t total_poses);
 

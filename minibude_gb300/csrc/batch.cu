@@ -87,6 +87,7 @@ int upload_batch(Context &c, const bude_atom *protein, int natpro, const bude_ff
                      (size_t)total_poses * sizeof(float), 6, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_error(e, "batch upload");
   c.have_batch = true;
+  ++c.batch_uploads;
   if (keep) return BUDE_OK;
   ++c.batch_gen;
   c.nligands = nligands;

@@ -14,6 +14,28 @@ struct Surrogate;
 struct ScreenState;
 struct StreamState;
 
+// CUDA events owned by one host call: created together, destroyed when the call returns by any
+// path.  ok() is false when a creation failed.
+struct EventSet {
+  std::vector<cudaEvent_t> ev;
+  explicit EventSet(size_t n, unsigned flags = cudaEventDefault) : ev(n, nullptr) {
+    for (auto &e : ev)
+      if (cudaEventCreateWithFlags(&e, flags) != cudaSuccess) e = nullptr;
+  }
+  ~EventSet() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  EventSet(const EventSet &) = delete;
+  EventSet &operator=(const EventSet &) = delete;
+  cudaEvent_t operator[](size_t i) const { return ev[i]; }
+  bool ok() const {
+    for (cudaEvent_t e : ev)
+      if (!e) return false;
+    return true;
+  }
+};
+
 // A growable device allocation.
 struct DevBuf {
   void *ptr = nullptr;
@@ -50,6 +72,7 @@ struct Context {
   cudaGraphExec_t graph = nullptr;
   bude_launch_cfg graph_cfg{};
   long long batch_gen = 0; // bumped whenever the batch's shape (ligand sizes, pose counts) changes
+  long long batch_uploads = 0; // bumped by every successful batch upload
   long long batch_tuned_key = -1;
   bude_launch_cfg batch_tuned{};
   float batch_tuned_ms = 0.f;

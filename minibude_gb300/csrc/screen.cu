@@ -319,6 +319,7 @@ struct ScreenState {
   DevBuf pose_off, flag, counts, comp_off, comp_pose, comp_xform, comp_exact, err, final_e, rescored, items, fb;
   DevBuf partial;             // slice sums of split exact evaluations
   cudaStream_t side = nullptr; // the exact rescoring beside the surrogate
+  long long result_for = -1;   // Context::batch_uploads of the batch the stored result belongs to
 };
 
 void release_screen(Context &c) {
@@ -375,6 +376,7 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
     return set_error(BUDE_ERR_ARG, "fractions must lie in [0, 1]");
   if (!c.screen) c.screen = new ScreenState();
   ScreenState &s = *c.screen;
+  s.result_for = -1; // a run that fails leaves no result behind
   const long long np = c.batch_poses;
   const int nl = c.nligands;
   int rc = s.pose_off.reserve((size_t)(nl + 1) * 8, "screen offsets");
@@ -454,10 +456,8 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
     cudaError_t es = cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking);
     if (es != cudaSuccess) return cuda_error(es, "screen rescoring stream");
   }
-  std::vector<cudaEvent_t> ready(nchunks);
-  for (auto &x : ready) cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
-  cudaEvent_t ev[5];
-  for (auto &e : ev) cudaEventCreate(&e);
+  EventSet ready((size_t)nchunks, cudaEventDisableTiming), ev(5);
+  if (!ready.ok() || !ev.ok()) return set_error(BUDE_ERR_CUDA, "could not create the screen's events");
   cudaEventRecord(ev[0], c.stream);
   cudaEventRecord(ev[1], c.stream); // re-recorded after each chunk's surrogate
   cudaMemcpyAsync(s.pose_off.ptr, c.pose_off.data(), (size_t)(nl + 1) * 8, cudaMemcpyHostToDevice, c.stream);
@@ -492,7 +492,7 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
                                s.comp_exact.as<float>(), s.partial.as<float>(), ncomp, rs, overlap ? 2 : 0, cfg.tile);
   }
   if (overlap) {
-    cudaEvent_t joined = ready.empty() ? nullptr : ready[0];
+    cudaEvent_t joined = nchunks > 0 ? ready[0] : nullptr;
     if (joined) {
       cudaEventRecord(joined, rs);
       cudaStreamWaitEvent(c.stream, joined, 0);
@@ -500,7 +500,6 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
   }
   cudaEventRecord(ev[2], c.stream);
   cudaError_t e = cudaStreamSynchronize(c.stream);
-  for (auto &x : ready) cudaEventDestroy(x);
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_error(e, "screen rescoring");
   // 4. audit and fallback
@@ -559,7 +558,7 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
     for (float v : err) mx = std::max(mx, v);
     stats->max_audit_error = mx;
   }
-  for (auto &x : ev) cudaEventDestroy(x);
+  s.result_for = c.batch_uploads;
   return BUDE_OK;
 }
 
@@ -577,8 +576,9 @@ int bude_screen_run(bude_gpu_ctx *ctx, const bude_screen_cfg *cfg, bude_screen_s
 
 int bude_screen_download(bude_gpu_ctx *ctx, float *final_energies, uint8_t *rescored, float *audit_error,
                          int64_t total_poses) {
-  if (!ctx || !ctx->screen || !ctx->have_batch || total_poses != ctx->batch_poses)
-    return set_error(BUDE_ERR_STATE, "no screen result for %lld poses", (long long)total_poses);
+  if (!ctx || !ctx->screen || !ctx->have_batch || ctx->screen->result_for != ctx->batch_uploads ||
+      total_poses != ctx->batch_poses)
+    return set_error(BUDE_ERR_STATE, "no screen result of the uploaded batch for %lld poses", (long long)total_poses);
   cudaSetDevice(ctx->device);
   cudaError_t e = cudaSuccess;
   if (final_energies && total_poses > 0)

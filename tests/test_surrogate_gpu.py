@@ -6,7 +6,7 @@ import pytest
 
 import surrogate_ref as ref
 from minibude_gb300 import SMALL, BatchSpec, synthetic_batch, synthetic_deck
-from minibude_gb300.capi import BUDE_ERR_ARG, BudeError
+from minibude_gb300.capi import BUDE_ERR_ARG, BUDE_ERR_STATE, BudeError
 from minibude_gb300.model import GpuContext, launch_cfg
 
 pytestmark = pytest.mark.gpu
@@ -184,6 +184,33 @@ def test_surrogate_errors(built_library):
         big_ff = np.concatenate([ff, ff, ff])
         with pytest.raises(BudeError):
             ctx.surrogate_init(protein, big_ff)  # 102 types > 64
+
+
+def test_screen_result_belongs_to_its_batch(built_library):
+    # A screen's result is downloadable until the next batch upload, even one of the same shape
+    # (whose poses differ); screening that batch gives a result again.
+    protein, ff = small_protein()
+    a = synthetic_batch(BatchSpec("t", 6, 16, 40, 200, 600), protein, ff, 21)
+    b = synthetic_batch(BatchSpec("t", 6, 16, 40, 200, 600), protein, ff, 22)
+    cfg = launch_cfg(8, 128, 1, 64, 2, cluster=0)
+    with GpuContext(0) as ctx:
+        ctx.upload_batch(a)
+        ctx.surrogate_init(protein, ff, seed=2)
+        ctx.screen(cfg, top_frac=0.05, audit_frac=0.05, audit_tol=1e9, seed=1)
+        fa, ra, _ = ctx.screen_download(a.nligands)
+        ctx.upload_batch(a)  # the same batch again: still a new upload
+        with pytest.raises(BudeError) as ei:
+            ctx.screen_download(a.nligands)
+        assert ei.value.code == BUDE_ERR_STATE
+        ctx.screen(cfg, top_frac=0.05, audit_frac=0.05, audit_tol=1e9, seed=1)
+        fa2, ra2, _ = ctx.screen_download(a.nligands)
+        assert np.array_equal(fa, fa2) and np.array_equal(ra, ra2)
+        ctx.upload_batch(b)
+        with pytest.raises(BudeError):
+            ctx.screen_download(b.nligands)
+        ctx.screen(cfg, top_frac=0.05, audit_frac=0.05, audit_tol=1e9, seed=1)
+        fb, _, _ = ctx.screen_download(b.nligands)
+        assert not np.array_equal(fa, fb)
 
 
 def test_screen_chunks_give_the_same_answer(built_library):
