@@ -118,7 +118,8 @@ int bude_gpu_run(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, float *kernel_ms
 int bude_gpu_run_many(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, int32_t iterations, int32_t flush_l2,
                       float *ms_per_iter, float *exact_ms_per_iter);
 
-/* Copy the energies of the last evaluation to the host (src/cuda/fasten.hpp:288-289). */
+/* Copy the energies of the last evaluation to the host (src/cuda/fasten.hpp:288-289).
+ * BUDE_ERR_STATE when no deck is uploaded (a failed upload or a batch upload leaves none). */
 int bude_gpu_download(bude_gpu_ctx *ctx, float *energies, int64_t nposes);
 
 /* End-to-end evaluation from host buffers: copies `poses` (and the ligand, when not NULL) to the
@@ -151,7 +152,8 @@ int bude_gpu_fasten(int device, int32_t ppwi, int32_t wgsize, const bude_atom *p
  * atoms [ligand_offsets[l], ligand_offsets[l+1]) of ligand_atoms and poses
  * [pose_offsets[l], pose_offsets[l+1]) of the [6][pose_stride] pose block; both offset arrays
  * have nligands+1 entries starting at 0.  A batch replaces any deck uploaded to the context (and
- * vice versa); energies come out in the concatenated pose order. */
+ * vice versa); energies come out in the concatenated pose order.  A batch holds at most
+ * 2^31 - 1 poses (work items index poses with 32-bit integers): BUDE_ERR_ARG beyond that. */
 int bude_gpu_upload_batch(bude_gpu_ctx *ctx, const bude_atom *protein, int32_t natpro,
                           const bude_ffparams *forcefield, int32_t ntypes, int32_t nligands,
                           const bude_atom *ligand_atoms, const int32_t *ligand_offsets, const float *poses,

@@ -59,6 +59,9 @@ int upload_batch(Context &c, const bude_atom *protein, int natpro, const bude_ff
   const long long total_poses = pose_off[nligands];
   if ((total_atoms > 0 && !atoms) || (total_poses > 0 && (!poses || pose_stride < total_poses)))
     return set_error(BUDE_ERR_ARG, "bad batch atoms or poses");
+  // Work items (batch, screen and surrogate) carry pose indices as 32-bit integers.
+  if (total_poses > 0x7fffffffLL)
+    return set_error(BUDE_ERR_ARG, "a batch holds at most 2^31 - 1 poses (got %lld)", total_poses);
   for (int i = 0; i < natpro; ++i)
     if (protein[i].type < 0 || protein[i].type >= ntypes)
       return set_error(BUDE_ERR_TYPE, "protein atom %d has type %d outside the forcefield (%d types)", i,

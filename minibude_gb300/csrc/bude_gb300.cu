@@ -556,6 +556,7 @@ int bude_gpu_run_many(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, int32_t ite
 
 int bude_gpu_download(bude_gpu_ctx *ctx, float *energies, int64_t nposes) {
   if (!ctx || (!energies && nposes > 0)) return set_error(BUDE_ERR_ARG, "NULL argument");
+  if (!ctx->have_deck) return set_error(BUDE_ERR_STATE, "no deck uploaded");
   if (nposes != ctx->nposes)
     return set_error(BUDE_ERR_ARG, "download of %lld energies but %lld poses are uploaded", (long long)nposes,
                      ctx->nposes);

@@ -173,6 +173,8 @@ class GpuContext:
         pose_off = np.ascontiguousarray(pose_off, np.int64)
         if poses.ndim != 2 or poses.shape[0] != 6 or poses.dtype != np.float32 or poses.strides[1] != 4:
             raise ValueError("poses must be a float32 [6][n] array with contiguous rows")
+        if len(pose_off) < 1 or pose_off[-1] != poses.shape[1]:
+            raise ValueError("the pose offsets must end at the number of poses")
         check(self._lib.bude_gpu_upload_batch(self.handle, ptr(protein), protein.size, ptr(ff), ff.size,
                                               len(lig_off) - 1, ptr(atoms), ptr(lig_off),
                                               ctypes.c_void_p(poses.ctypes.data), poses.strides[0] // 4,

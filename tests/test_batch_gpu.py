@@ -164,6 +164,25 @@ def test_batch_errors(ctx):
         ctx.run_batch(launch_cfg(8, 128))
 
 
+def test_batch_pose_limit(ctx):
+    # Work items index poses with 32-bit integers: a batch of 2^31 poses is refused before any pose
+    # is read (a one-pose buffer stands in for the poses; nothing reads past it).
+    from minibude_gb300 import capi
+    from minibude_gb300.model import _atoms, _ff
+    b = small_batch(n=1)
+    prot, ff, atoms = _atoms(b.protein), _ff(b.forcefield), _atoms(b.ligands[0])
+    lig_off = np.array([0, atoms.size], np.int32)
+    pose_off = np.array([0, 2 ** 31], np.int64)
+    one = np.zeros(6, np.float32)
+    rc = capi.lib().bude_gpu_upload_batch(ctx.handle, capi.ptr(prot), prot.size, capi.ptr(ff), ff.size, 1,
+                                          capi.ptr(atoms), capi.ptr(lig_off), capi.ptr(one), 2 ** 31,
+                                          capi.ptr(pose_off))
+    assert rc == BUDE_ERR_ARG and "2^31" in capi.last_error()
+    with pytest.raises(BudeError) as ei:
+        ctx.run_batch(launch_cfg(8, 128))
+    assert ei.value.code == BUDE_ERR_STATE
+
+
 def _reshaped(b, seed, poses_shift=0):
     """A batch of the same ligand sizes with other coordinates; poses_shift moves poses between the
     first two ligands (same ligand count and total pose count, another shape)."""

@@ -166,6 +166,9 @@ def test_errors(ctx):
     with pytest.raises(BudeError) as ei:
         ctx.run(launch_cfg(8, 128, 1, 64))  # the failed upload left no deck
     assert ei.value.code == BUDE_ERR_STATE
+    with pytest.raises(BudeError) as ei:
+        ctx.download()  # nor energies to read back
+    assert ei.value.code == BUDE_ERR_STATE
     ctx.upload(deck)
     for cfg in (launch_cfg(3, 128, 1, 64), launch_cfg(8, 100, 1, 64), launch_cfg(8, 128, 9, 64),
                 launch_cfg(8, 128, 1, 12), launch_cfg(8, 1024, 1, 64), launch_cfg(8, 128, 1, 64, 3),
