@@ -84,10 +84,10 @@ int upload_batch(Context &c, const bude_atom *protein, int natpro, const bude_ff
   if (!rc) rc = c.b_counter.reserve(256, "batch work counter");
   if (rc) return rc;
   cudaError_t e = cudaSuccess;
-  if (total_atoms > 0) e = cudaMemcpy(c.b_ligands.ptr, atoms, (size_t)total_atoms * 16, cudaMemcpyHostToDevice);
+  if (total_atoms > 0) e = copy_sync(c, c.b_ligands.ptr, atoms, (size_t)total_atoms * 16, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && total_poses > 0)
-    e = cudaMemcpy2D(c.b_poses.ptr, (size_t)total_poses * sizeof(float), poses, (size_t)pose_stride * sizeof(float),
-                     (size_t)total_poses * sizeof(float), 6, cudaMemcpyHostToDevice);
+    e = copy2d_sync(c, c.b_poses.ptr, (size_t)total_poses * sizeof(float), poses, (size_t)pose_stride * sizeof(float),
+                    (size_t)total_poses * sizeof(float), 6, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_error(e, "batch upload");
   c.have_batch = true;
   ++c.batch_uploads;
@@ -128,7 +128,7 @@ static int build_items(Context &c, int ppwi, int wgsize, std::vector<int4> *keep
   int rc = c.b_items.reserve(std::max<size_t>(items.size(), 1) * sizeof(int4), "batch items");
   if (rc) return rc;
   if (!items.empty()) {
-    cudaError_t e = cudaMemcpy(c.b_items.ptr, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice);
+    cudaError_t e = copy_sync(c, c.b_items.ptr, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_error(e, "batch item upload");
   }
   c.n_items = (int)items.size();
@@ -391,7 +391,11 @@ int autotune_batch(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms
     if (picked.empty()) continue;
     rc = sub.reserve(picked.size() * sizeof(int4), "autotune items");
     if (rc) break;
-    cudaMemcpy(sub.ptr, picked.data(), picked.size() * sizeof(int4), cudaMemcpyHostToDevice);
+    const cudaError_t ec = copy_sync(c, sub.ptr, picked.data(), picked.size() * sizeof(int4), cudaMemcpyHostToDevice);
+    if (ec != cudaSuccess) {
+      rc = cuda_error(ec, "autotune item upload");
+      break;
+    }
     rc = enqueue_persistent(c, cfg, grid, sub.as<int4>(), (int)picked.size()); // warm-up
     cudaEventRecord(e0, c.stream);
     if (!rc) rc = enqueue_persistent(c, cfg, grid, sub.as<int4>(), (int)picked.size());

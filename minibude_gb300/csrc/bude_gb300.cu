@@ -36,6 +36,25 @@ int set_error(int code, const char *fmt, ...) {
   return code;
 }
 
+cudaError_t copy_sync(const Context &c, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind) {
+  if (bytes == 0) return cudaSuccess;
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, c.stream);
+  return e == cudaSuccess ? cudaStreamSynchronize(c.stream) : e;
+}
+
+cudaError_t copy2d_sync(const Context &c, void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
+                        size_t height, cudaMemcpyKind kind) {
+  if (width == 0 || height == 0) return cudaSuccess;
+  cudaError_t e = cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, c.stream);
+  return e == cudaSuccess ? cudaStreamSynchronize(c.stream) : e;
+}
+
+cudaError_t fill_sync(const Context &c, void *dst, int value, size_t bytes) {
+  if (bytes == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(dst, value, bytes, c.stream);
+  return e == cudaSuccess ? cudaStreamSynchronize(c.stream) : e;
+}
+
 int cuda_error(cudaError_t e, const char *what) {
   return set_error(BUDE_ERR_CUDA, "%s: %s: %s", what, cudaGetErrorName(e), cudaGetErrorString(e));
 }
@@ -73,7 +92,7 @@ int ensure_slab(Context &c, const bude_atom *protein, int natpro, const bude_ffp
   build_slab(protein, natpro, ff, ntypes, c.natpro_pad, slab);
   int rc = c.slab.reserve(slab.size() * sizeof(float), "slab");
   if (rc) return rc;
-  cudaError_t e = cudaMemcpy(c.slab.ptr, slab.data(), slab.size() * sizeof(float), cudaMemcpyHostToDevice);
+  cudaError_t e = copy_sync(c, c.slab.ptr, slab.data(), slab.size() * sizeof(float), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_error(e, "slab upload");
   c.slab_key = std::move(key);
   if (rebuilt) *rebuilt = true;

@@ -87,6 +87,14 @@ struct Context {
   std::vector<unsigned char> slab_key;
 };
 
+// Copies and fills ordered on the context's stream and finished on return.  The context's stream
+// is non-blocking, so plain cudaMemcpy / cudaMemset (the legacy default stream) would be ordered
+// neither after the kernels already on it nor before the ones launched next.
+cudaError_t copy_sync(const Context &c, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind);
+cudaError_t copy2d_sync(const Context &c, void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
+                        size_t height, cudaMemcpyKind kind);
+cudaError_t fill_sync(const Context &c, void *dst, int value, size_t bytes);
+
 int set_error(int code, const char *fmt, ...);
 int cuda_error(cudaError_t e, const char *what);
 const char *last_error();

@@ -582,11 +582,11 @@ int bude_screen_download(bude_gpu_ctx *ctx, float *final_energies, uint8_t *resc
   cudaSetDevice(ctx->device);
   cudaError_t e = cudaSuccess;
   if (final_energies && total_poses > 0)
-    e = cudaMemcpy(final_energies, ctx->screen->final_e.ptr, (size_t)total_poses * 4, cudaMemcpyDeviceToHost);
+    e = copy_sync(*ctx, final_energies, ctx->screen->final_e.ptr, (size_t)total_poses * 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && rescored && total_poses > 0)
-    e = cudaMemcpy(rescored, ctx->screen->rescored.ptr, (size_t)total_poses, cudaMemcpyDeviceToHost);
+    e = copy_sync(*ctx, rescored, ctx->screen->rescored.ptr, (size_t)total_poses, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && audit_error && ctx->nligands > 0)
-    e = cudaMemcpy(audit_error, ctx->screen->err.ptr, (size_t)ctx->nligands * 4, cudaMemcpyDeviceToHost);
+    e = copy_sync(*ctx, audit_error, ctx->screen->err.ptr, (size_t)ctx->nligands * 4, cudaMemcpyDeviceToHost);
   return e == cudaSuccess ? BUDE_OK : cuda_error(e, "screen download");
 }
 

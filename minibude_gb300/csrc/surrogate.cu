@@ -227,9 +227,9 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
   if (!rc) rc = s.w3_bf.reserve(kHid * kHid * 2, "w3 bf16");
   if (!rc) rc = s.w3t_bf.reserve(kHid * kHid * 2, "w3t bf16");
   if (rc) return rc;
-  cudaError_t e = cudaMemcpy(s.params.ptr, p.data(), pb, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemset(s.adam_m.ptr, 0, pb);
-  if (e == cudaSuccess) e = cudaMemset(s.adam_v.ptr, 0, pb);
+  cudaError_t e = copy_sync(c, s.params.ptr, p.data(), pb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = fill_sync(c, s.adam_m.ptr, 0, pb);
+  if (e == cudaSuccess) e = fill_sync(c, s.adam_v.ptr, 0, pb);
   if (e != cudaSuccess) return cuda_error(e, "surrogate init");
 
   // Field grid over [-extent, extent]^3.
@@ -241,8 +241,13 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
   if (!rc) rc = dff.reserve((size_t)ntypes * sizeof(bude_ffparams), "grid forcefield");
   if (!rc) rc = inv.reserve(16 * sizeof(float), "grid scales");
   if (rc) return rc;
-  if (natpro > 0) cudaMemcpy(s.protein4.ptr, protein, (size_t)natpro * 16, cudaMemcpyHostToDevice);
-  cudaMemcpy(dff.ptr, ff, (size_t)ntypes * sizeof(bude_ffparams), cudaMemcpyHostToDevice);
+  e = copy_sync(c, s.protein4.ptr, protein, (size_t)natpro * 16, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = copy_sync(c, dff.ptr, ff, (size_t)ntypes * sizeof(bude_ffparams), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    dff.release();
+    inv.release();
+    return cuda_error(e, "grid inputs");
+  }
   GridBuild gb;
   gb.protein = s.protein4.as<float4>();
   gb.ff = dff.as<bude_ffparams>();
@@ -260,7 +265,12 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
   }
   // Unit standard deviation per channel (a zero channel keeps scale 1).
   std::vector<float> h((size_t)nvox * 16);
-  cudaMemcpy(h.data(), s.grid.ptr, h.size() * sizeof(float), cudaMemcpyDeviceToHost);
+  e = copy_sync(c, h.data(), s.grid.ptr, h.size() * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    dff.release();
+    inv.release();
+    return cuda_error(e, "field grid read-back");
+  }
   float scale[16];
   for (int k = 0; k < 16; ++k) {
     double m = 0, m2 = 0;
@@ -273,7 +283,12 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
     const double var = std::max(0.0, m2 / (double)nvox - m * m);
     scale[k] = var > 1e-12 ? (float)(1.0 / std::sqrt(var)) : 1.f;
   }
-  cudaMemcpy(inv.ptr, scale, sizeof scale, cudaMemcpyHostToDevice);
+  e = copy_sync(c, inv.ptr, scale, sizeof scale, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    dff.release();
+    inv.release();
+    return cuda_error(e, "grid scales");
+  }
   grid_scale_kernel<<<(unsigned)((nvox * 16 + 255) / 256), 256, 0, c.stream>>>(s.grid.as<float>(), nvox,
                                                                              inv.as<float>());
   e = cudaStreamSynchronize(c.stream);
@@ -415,8 +430,9 @@ static int upload_pose_ligands(Context &c, Surrogate &s, std::vector<int> &lig_n
   if (!rc) rc = s.pose_lig_n.reserve((size_t)std::max(np, 1LL) * 4, "pose ligands");
   if (rc) return rc;
   if (np > 0) {
-    cudaMemcpy(s.pose_lig_first.ptr, first.data(), (size_t)np * 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(s.pose_lig_n.ptr, lig_n.data(), (size_t)np * 4, cudaMemcpyHostToDevice);
+    cudaError_t e = copy_sync(c, s.pose_lig_first.ptr, first.data(), (size_t)np * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = copy_sync(c, s.pose_lig_n.ptr, lig_n.data(), (size_t)np * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_error(e, "pose ligands");
   }
   return BUDE_OK;
 }
@@ -451,7 +467,8 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
   int rc = s.labels.reserve((size_t)np * 4, "labels");
   if (rc) return rc;
   if (labels) {
-    cudaMemcpy(s.labels.ptr, labels, (size_t)np * 4, cudaMemcpyHostToDevice);
+    const cudaError_t e = copy_sync(c, s.labels.ptr, labels, (size_t)np * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_error(e, "labels");
   } else {
     // Labels: exact energies of every pose from the batched exact kernel.
     bude_launch_cfg cfg{16, 128, 1, 64, 1, 0};
@@ -467,14 +484,16 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
   // b4 starts at the mean label per ligand atom.
   if (s.step == 0) {
     std::vector<float> hl((size_t)np);
-    cudaMemcpy(hl.data(), s.labels.ptr, (size_t)np * 4, cudaMemcpyDeviceToHost);
+    cudaError_t e = copy_sync(c, hl.data(), s.labels.ptr, (size_t)np * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, "labels read-back");
     double sl = 0, sa = 0;
     for (long long p = 0; p < np; ++p) {
       sl += std::asinh(hl[(size_t)p] / kLossScale) * kLossScale;
       sa += lig_n[(size_t)p];
     }
     const float b4 = (float)(sl / std::max(sa, 1.0));
-    cudaMemcpy(s.params.as<float>() + kOffB4, &b4, sizeof b4, cudaMemcpyHostToDevice);
+    e = copy_sync(c, s.params.as<float>() + kOffB4, &b4, sizeof b4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_error(e, "output bias");
   }
   const int nb_full = (int)std::min<long long>(batch, np);
   const int steps_per_epoch = (int)((np + nb_full - 1) / nb_full);
@@ -523,7 +542,8 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
       ++done;
       if (!rc && ep == epochs - 1) {
         std::vector<float> lh((size_t)nb);
-        cudaMemcpy(lh.data(), s.loss.ptr, (size_t)nb * 4, cudaMemcpyDeviceToHost);
+        const cudaError_t e = copy_sync(c, lh.data(), s.loss.ptr, (size_t)nb * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = cuda_error(e, "loss read-back");
         for (float v : lh) loss_sum += v;
       }
     }
@@ -552,21 +572,23 @@ int surrogate_gradient(Context &c, const int *poses, int n, const float *labels,
   if (!rc) rc = s.epoch_pose.reserve((size_t)n * 4, "poses");
   if (!rc) rc = s.epoch_rowoff.reserve((size_t)(n + 1) * 4, "row offsets");
   if (rc) return rc;
-  cudaMemcpy(s.labels.ptr, labels, (size_t)np * 4, cudaMemcpyHostToDevice);
+  cudaError_t e = copy_sync(c, s.labels.ptr, labels, (size_t)np * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_error(e, "labels");
   std::vector<int> ro(n + 1, 0);
   for (int i = 0; i < n; ++i) {
     if (poses[i] < 0 || poses[i] >= np) return set_error(BUDE_ERR_ARG, "pose index out of range");
     ro[i + 1] = ro[i] + lig_n[(size_t)poses[i]];
   }
-  cudaMemcpy(s.epoch_pose.ptr, poses, (size_t)n * 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(s.epoch_rowoff.ptr, ro.data(), ro.size() * 4, cudaMemcpyHostToDevice);
+  e = copy_sync(c, s.epoch_pose.ptr, poses, (size_t)n * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = copy_sync(c, s.epoch_rowoff.ptr, ro.data(), ro.size() * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_error(e, "gradient rows");
   rc = train_step(c, s, s.epoch_pose.as<int>(), s.epoch_rowoff.as<int>(), n, ro[n], 0.f, nullptr);
-  cudaError_t e = cudaStreamSynchronize(c.stream);
+  e = cudaStreamSynchronize(c.stream);
   if (!rc && e != cudaSuccess) rc = cuda_error(e, "surrogate gradient");
   if (rc) return rc;
-  if (grad_out) cudaMemcpy(grad_out, s.grads.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
-  if (pred_out) cudaMemcpy(pred_out, s.pred.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost);
-  return BUDE_OK;
+  if (grad_out) e = copy_sync(c, grad_out, s.grads.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && pred_out) e = copy_sync(c, pred_out, s.pred.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "gradient read-back");
 }
 
 // Features (as floats) and atom types of the rows of the given poses; for inspection and tests.
@@ -588,8 +610,9 @@ int surrogate_features(Context &c, const int *poses, int n, float *X, int *types
   if (!rc) rc = s.epoch_rowoff.reserve((size_t)(n + 1) * 4, "row offsets");
   if (!rc) rc = ensure_train_scratch(s, std::max(rows, 1LL), n, 1, 1);
   if (rc) return rc;
-  cudaMemcpy(s.epoch_pose.ptr, poses, (size_t)n * 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(s.epoch_rowoff.ptr, ro.data(), ro.size() * 4, cudaMemcpyHostToDevice);
+  cudaError_t e = copy_sync(c, s.epoch_pose.ptr, poses, (size_t)n * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = copy_sync(c, s.epoch_rowoff.ptr, ro.data(), ro.size() * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_error(e, "feature rows");
   RowMap m;
   m.pose = s.epoch_pose.as<int>();
   m.row_off = s.epoch_rowoff.as<int>();
@@ -599,16 +622,17 @@ int surrogate_features(Context &c, const int *poses, int n, float *X, int *types
   train_features_kernel<<<(n * 32 + 255) / 256, 256, 0, c.stream>>>(weights(s), s.fg, c.b_ligands.as<float4>(),
                                                                       c.b_xform.as<float4>(), m,
                                                                       s.X.as<__nv_bfloat16>(), s.row_type.as<int>());
-  cudaError_t e = cudaStreamSynchronize(c.stream);
+  e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return cuda_error(e, "surrogate features");
   std::vector<uint16_t> xb((size_t)rows * kFeat);
-  cudaMemcpy(xb.data(), s.X.ptr, xb.size() * 2, cudaMemcpyDeviceToHost);
+  e = copy_sync(c, xb.data(), s.X.ptr, xb.size() * 2, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "feature read-back");
   for (size_t i = 0; i < xb.size(); ++i) {
     const uint32_t u = (uint32_t)xb[i] << 16;
     std::memcpy(&X[i], &u, 4);
   }
-  if (types) cudaMemcpy(types, s.row_type.ptr, (size_t)rows * 4, cudaMemcpyDeviceToHost);
-  return BUDE_OK;
+  if (types) e = copy_sync(c, types, s.row_type.ptr, (size_t)rows * 4, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? BUDE_OK : cuda_error(e, "row type read-back");
 }
 
 // Scoring items (128 poses of one ligand each, ligand by ligand) and, unless the caller already
@@ -632,7 +656,8 @@ int surrogate_prepare(Context &c, bool xform_ready) {
     }
     rc = s.items.reserve(std::max<size_t>(items.size(), 1) * sizeof(int4), "surrogate items");
     if (rc) return rc;
-    if (!items.empty()) cudaMemcpy(s.items.ptr, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice);
+    const cudaError_t e = copy_sync(c, s.items.ptr, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_error(e, "surrogate items");
     s.n_items = (int)items.size();
     s.items_for = c.batch_gen;
   }
@@ -694,13 +719,15 @@ int surrogate_io(Context &c, float *out, const float *in, long long n) {
   Surrogate &s = sur(c);
   if (!s.ready) return set_error(BUDE_ERR_STATE, "surrogate not initialised");
   if (n != kNParams) return set_error(BUDE_ERR_ARG, "parameter vector has %lld values, not %lld", n, kNParams);
-  if (out) cudaMemcpy(out, s.params.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaSuccess;
+  if (out) e = copy_sync(c, out, s.params.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && in) e = copy_sync(c, s.params.ptr, in, kNParams * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_error(e, "surrogate parameters");
   if (in) {
-    cudaMemcpy(s.params.ptr, in, kNParams * 4, cudaMemcpyHostToDevice);
     int rc = publish(c, s);
     if (rc) return rc;
   }
-  cudaError_t e = cudaStreamSynchronize(c.stream);
+  e = cudaStreamSynchronize(c.stream);
   return e == cudaSuccess ? BUDE_OK : cuda_error(e, "surrogate parameters");
 }
 
@@ -709,9 +736,10 @@ int surrogate_save(Context &c, const char *path) {
   Surrogate &s = sur(c);
   if (!s.ready) return set_error(BUDE_ERR_STATE, "surrogate not initialised");
   std::vector<float> buf(3 * kNParams);
-  cudaMemcpy(buf.data(), s.params.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
-  cudaMemcpy(buf.data() + kNParams, s.adam_m.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
-  cudaMemcpy(buf.data() + 2 * kNParams, s.adam_v.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  cudaError_t e = copy_sync(c, buf.data(), s.params.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = copy_sync(c, buf.data() + kNParams, s.adam_m.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = copy_sync(c, buf.data() + 2 * kNParams, s.adam_v.ptr, kNParams * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "checkpoint read-back");
   FILE *f = std::fopen(path, "wb");
   if (!f) return set_error(BUDE_ERR_ARG, "cannot write %s", path);
   const unsigned long long hdr[3] = {0x4255444553555231ull /* "BUDESUR1" */, (unsigned long long)kNParams,
@@ -732,9 +760,10 @@ int surrogate_load(Context &c, const char *path) {
             hdr[1] == (unsigned long long)kNParams && std::fread(buf.data(), 4, buf.size(), f) == buf.size();
   std::fclose(f);
   if (!ok) return set_error(BUDE_ERR_ARG, "%s is not a surrogate checkpoint of this model", path);
-  cudaMemcpy(s.params.ptr, buf.data(), kNParams * 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(s.adam_m.ptr, buf.data() + kNParams, kNParams * 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(s.adam_v.ptr, buf.data() + 2 * kNParams, kNParams * 4, cudaMemcpyHostToDevice);
+  cudaError_t e = copy_sync(c, s.params.ptr, buf.data(), kNParams * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = copy_sync(c, s.adam_m.ptr, buf.data() + kNParams, kNParams * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = copy_sync(c, s.adam_v.ptr, buf.data() + 2 * kNParams, kNParams * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_error(e, "checkpoint upload");
   s.step = (long long)hdr[2];
   return publish(c, s);
 }
@@ -785,7 +814,8 @@ int bude_surrogate_download(bude_gpu_ctx *ctx, float *scores, int64_t n) {
   float *d = surrogate_scores(*ctx);
   if (!d || !ctx->have_batch || n != ctx->batch_poses)
     return set_error(BUDE_ERR_ARG, "no surrogate scores for %lld poses", (long long)n);
-  cudaError_t e = cudaMemcpy(scores, d, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  cudaSetDevice(ctx->device);
+  cudaError_t e = copy_sync(*ctx, scores, d, (size_t)n * 4, cudaMemcpyDeviceToHost);
   return e == cudaSuccess ? BUDE_OK : cuda_error(e, "score download");
 }
 

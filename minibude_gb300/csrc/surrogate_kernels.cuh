@@ -650,8 +650,29 @@ __global__ void __launch_bounds__(kMlpThreads) train_backward_kernel(BwdArgs a) 
         s.type[lr1] = v1 ? a.row_type[r1] : 0;
       }
       __syncthreads();
-      if (threadIdx.x < kEmb) { // thread j owns embedding column j: rows in order
-        for (int r = 0; r < kRowsPerCta; ++r) s.emb_acc[s.type[r]][threadIdx.x] += s.demb[r][threadIdx.x];
+      {
+        // Thread (type group tg, column c) owns the accumulators of types tg, tg+16, tg+32, tg+48
+        // in column c and adds the tile's rows of those types in row order: every accumulator
+        // sees the same additions in the same order as one thread per column walking all rows.
+        static_assert(kMaxTypes == 64 && kEmb == 16 && kMlpThreads == 256, "type groups assume 64 x 16 / 256");
+        const int c = threadIdx.x & (kEmb - 1), tg = threadIdx.x / kEmb;
+        float e0 = s.emb_acc[tg][c], e1 = s.emb_acc[tg + 16][c], e2 = s.emb_acc[tg + 32][c],
+              e3 = s.emb_acc[tg + 48][c];
+        for (int r = 0; r < kRowsPerCta; ++r) {
+          const int ty = s.type[r];
+          if ((ty & 15) != tg) continue;
+          const float d = s.demb[r][c];
+          switch (ty >> 4) {
+          case 0: e0 += d; break;
+          case 1: e1 += d; break;
+          case 2: e2 += d; break;
+          default: e3 += d; break;
+          }
+        }
+        s.emb_acc[tg][c] = e0;
+        s.emb_acc[tg + 16][c] = e1;
+        s.emb_acc[tg + 32][c] = e2;
+        s.emb_acc[tg + 48][c] = e3;
       }
       __syncthreads();
     }
@@ -675,9 +696,13 @@ struct WgradArgs {
   float *part;    // [chunks][128][kin]
 };
 
+// Rows per shared-memory stage of wgrad_kernel: four 16-row k-steps, so one pair of barriers
+// serves four MMA steps and the next stage's loads are in flight while this one computes.
+constexpr int kWgRows = 64;
+
 struct WgradSmem {
-  __nv_bfloat16 dz[16 * kLdH];
-  __nv_bfloat16 h[16 * kLdH];
+  __nv_bfloat16 dz[kWgRows * kLdH];
+  __nv_bfloat16 h[kWgRows * kLdH];
 };
 
 template <int KIN>
@@ -685,54 +710,81 @@ __global__ void __launch_bounds__(kMlpThreads) wgrad_kernel(WgradArgs a) {
   __shared__ __align__(16) WgradSmem s;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   constexpr int nt = KIN / 8; // n-tiles of the output row
+  constexpr int kDzVec = kWgRows * kHid / 8;   // 16-byte vectors of dZ per stage
+  constexpr int kHVec = kWgRows * KIN / 8;     // and of H
+  constexpr int kDzPer = kDzVec / kMlpThreads; // per thread
+  constexpr int kHPer = (kHVec + kMlpThreads - 1) / kMlpThreads;
+  static_assert(kDzVec % kMlpThreads == 0, "dZ stage must split evenly over the block");
   float acc[16][4];
 #pragma unroll
   for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
   const int r_begin = blockIdx.x * a.chunk_rows;
   const int r_end = min(a.rows, r_begin + a.chunk_rows);
-  for (int r = r_begin; r < r_end; r += 16) {
-    __syncthreads();
-    // stage 16 rows of dZ (128 wide) and of H (kin wide)
-    for (int i = threadIdx.x; i < 16 * kHid / 8; i += blockDim.x) {
+  // Registers holding the next stage: rows past r_end are zero (as the staging always did).
+  uint4 pd[kDzPer], ph[kHPer];
+  auto fetch = [&](int r) {
+#pragma unroll
+    for (int q = 0; q < kDzPer; ++q) {
+      const int i = threadIdx.x + q * kMlpThreads;
       const int rr = i / (kHid / 8), k8 = i % (kHid / 8);
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (r + rr < r_end) v = *reinterpret_cast<const uint4 *>(a.dZ + (long long)(r + rr) * kHid + k8 * 8);
-      *reinterpret_cast<uint4 *>(&s.dz[rr * kLdH + k8 * 8]) = v;
+      pd[q] = make_uint4(0, 0, 0, 0);
+      if (r + rr < r_end) pd[q] = *reinterpret_cast<const uint4 *>(a.dZ + (long long)(r + rr) * kHid + k8 * 8);
     }
-    for (int i = threadIdx.x; i < 16 * KIN / 8; i += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < kHPer; ++q) {
+      const int i = threadIdx.x + q * kMlpThreads;
       const int rr = i / (KIN / 8), k8 = i % (KIN / 8);
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (r + rr < r_end) {
-        v = *reinterpret_cast<const uint4 *>(a.Hin + (long long)(r + rr) * KIN + k8 * 8);
+      ph[q] = make_uint4(0, 0, 0, 0);
+      if (i < kHVec && r + rr < r_end) {
+        uint4 v = *reinterpret_cast<const uint4 *>(a.Hin + (long long)(r + rr) * KIN + k8 * 8);
         if (a.apply_act) {
           uint32_t *w = reinterpret_cast<uint32_t *>(&v);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float2 f = unpack_bf16(w[q]);
-            w[q] = act_pair(f.x, f.y);
+          for (int e = 0; e < 4; ++e) {
+            const float2 f = unpack_bf16(w[e]);
+            w[e] = act_pair(f.x, f.y);
           }
         }
+        ph[q] = v;
       }
-      *reinterpret_cast<uint4 *>(&s.h[rr * kLdH + k8 * 8]) = v;
     }
-    __syncthreads();
-    // A (m = out row, k = data row) = dZ^T: transposed 8x8 loads of dz[r][o].
-    uint32_t af[4];
-    {
-      const int q = lane >> 3;
-      const int row = (lane & 7) + ((q >> 1) << 3);
-      const int col = warp * 16 + ((q & 1) << 3);
-      ldsm_x4_trans(af, s.dz + row * kLdH + col);
+  };
+  if (r_begin < r_end) fetch(r_begin);
+  for (int r = r_begin; r < r_end; r += kWgRows) {
+    __syncthreads(); // the previous stage has been read
+#pragma unroll
+    for (int q = 0; q < kDzPer; ++q) {
+      const int i = threadIdx.x + q * kMlpThreads;
+      *reinterpret_cast<uint4 *>(&s.dz[(i / (kHid / 8)) * kLdH + (i % (kHid / 8)) * 8]) = pd[q];
     }
 #pragma unroll
-    for (int jp = 0; jp < nt / 2; ++jp) {
-      uint32_t b[4];
-      const int q = lane >> 3;
-      const int row = (lane & 7) + ((q & 1) << 3);
-      const int col = jp * 16 + ((q >> 1) << 3);
-      ldsm_x4_trans(b, s.h + row * kLdH + col);
-      mma_bf16(acc[2 * jp], af, b[0], b[1]);
-      mma_bf16(acc[2 * jp + 1], af, b[2], b[3]);
+    for (int q = 0; q < kHPer; ++q) {
+      const int i = threadIdx.x + q * kMlpThreads;
+      if (i < kHVec) *reinterpret_cast<uint4 *>(&s.h[(i / (KIN / 8)) * kLdH + (i % (KIN / 8)) * 8]) = ph[q];
+    }
+    __syncthreads();
+    if (r + kWgRows < r_end) fetch(r + kWgRows);
+    // 16-row k-steps in row order, none past r_end: the same MMA sequence as one stage per step.
+    for (int ks = 0; ks < kWgRows / 16 && r + ks * 16 < r_end; ++ks) {
+      const __nv_bfloat16 *dz = s.dz + ks * 16 * kLdH, *h = s.h + ks * 16 * kLdH;
+      // A (m = out row, k = data row) = dZ^T: transposed 8x8 loads of dz[r][o].
+      uint32_t af[4];
+      {
+        const int q = lane >> 3;
+        const int row = (lane & 7) + ((q >> 1) << 3);
+        const int col = warp * 16 + ((q & 1) << 3);
+        ldsm_x4_trans(af, dz + row * kLdH + col);
+      }
+#pragma unroll
+      for (int jp = 0; jp < nt / 2; ++jp) {
+        uint32_t b[4];
+        const int q = lane >> 3;
+        const int row = (lane & 7) + ((q & 1) << 3);
+        const int col = jp * 16 + ((q >> 1) << 3);
+        ldsm_x4_trans(b, h + row * kLdH + col);
+        mma_bf16(acc[2 * jp], af, b[0], b[1]);
+        mma_bf16(acc[2 * jp + 1], af, b[2], b[3]);
+      }
     }
   }
   float *out = a.part + (long long)blockIdx.x * kHid * KIN;
@@ -747,11 +799,20 @@ __global__ void __launch_bounds__(kMlpThreads) wgrad_kernel(WgradArgs a) {
 }
 
 // grad[i] = sum over parts of part[p][i], in part order.
+// Eight parts are loaded ahead of their adds, which stay in part order.
 __global__ void reduce_parts_kernel(const float *part, int nparts, long long n, long long stride, float *grad) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float v = 0.f;
-  for (int p = 0; p < nparts; ++p) v += part[p * stride + i];
+  int p = 0;
+  for (; p + 8 <= nparts; p += 8) {
+    float x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = part[(long long)(p + j) * stride + i];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v += x[j];
+  }
+  for (; p < nparts; ++p) v += part[(long long)p * stride + i];
   grad[i] = v;
 }
 
