@@ -650,29 +650,8 @@ __global__ void __launch_bounds__(kMlpThreads) train_backward_kernel(BwdArgs a) 
         s.type[lr1] = v1 ? a.row_type[r1] : 0;
       }
       __syncthreads();
-      {
-        // Thread (type group tg, column c) owns the accumulators of types tg, tg+16, tg+32, tg+48
-        // in column c and adds the tile's rows of those types in row order: every accumulator
-        // sees the same additions in the same order as one thread per column walking all rows.
-        static_assert(kMaxTypes == 64 && kEmb == 16 && kMlpThreads == 256, "type groups assume 64 x 16 / 256");
-        const int c = threadIdx.x & (kEmb - 1), tg = threadIdx.x / kEmb;
-        float e0 = s.emb_acc[tg][c], e1 = s.emb_acc[tg + 16][c], e2 = s.emb_acc[tg + 32][c],
-              e3 = s.emb_acc[tg + 48][c];
-        for (int r = 0; r < kRowsPerCta; ++r) {
-          const int ty = s.type[r];
-          if ((ty & 15) != tg) continue;
-          const float d = s.demb[r][c];
-          switch (ty >> 4) {
-          case 0: e0 += d; break;
-          case 1: e1 += d; break;
-          case 2: e2 += d; break;
-          default: e3 += d; break;
-          }
-        }
-        s.emb_acc[tg][c] = e0;
-        s.emb_acc[tg + 16][c] = e1;
-        s.emb_acc[tg + 32][c] = e2;
-        s.emb_acc[tg + 48][c] = e3;
+      if (threadIdx.x < kEmb) { // thread j owns embedding column j: rows in order
+        for (int r = 0; r < kRowsPerCta; ++r) s.emb_acc[s.type[r]][threadIdx.x] += s.demb[r][threadIdx.x];
       }
       __syncthreads();
     }
