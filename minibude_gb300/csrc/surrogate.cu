@@ -132,6 +132,11 @@ static int set_smem_limits() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(train_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(BwdSmem));
+  // Two backward blocks per SM (launch bounds cap the registers at 128): the shared-memory
+  // carveout must hold both.
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(train_backward_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return cuda_error(e, "surrogate shared-memory limits");
   done = true;
   return BUDE_OK;

@@ -488,7 +488,7 @@ struct BwdSmem {
   float emb_acc[kMaxTypes][kEmb];
 };
 
-__global__ void __launch_bounds__(kMlpThreads) train_backward_kernel(BwdArgs a) {
+__global__ void __launch_bounds__(kMlpThreads, 2) train_backward_kernel(BwdArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   BwdSmem &s = *reinterpret_cast<BwdSmem *>(smem_raw);
   for (int i = threadIdx.x; i < kHid * kHid / 8; i += blockDim.x) {
