@@ -289,17 +289,20 @@ int bude_gpu_selftest_wait(bude_gpu_ctx *ctx, int32_t limit_us, float *elapsed_m
  * the reference.  It is for callers that may not allocate GPU memory themselves: code running
  * inside another framework whose allocator owns the device heap, plugin hosts that hand a plugin
  * its buffers, and loops where cudaMalloc/cudaFree and their device synchronisation are not
- * allowed.  Every pointer is a DEVICE buffer on the current device: protein, ligand (16-byte
- * aligned) and forcefield records, poses as six float fields at poses + k*pose_stride, and the
- * output energies[nposes].  `stream` is a cudaStream_t (NULL: the default stream); the call
- * returns after the energies are written.  The working memory (per-deck protein slab, pose
- * transforms, an error word) is one fixed device array inside the library of about 11 MiB, held
- * by every GPU that loads it until the process exits: sizes above BUDE_NOALLOC_MAX_POSES poses or
- * BUDE_NOALLOC_MAX_SLAB_RECORDS slab records (forcefield types x protein atoms rounded up to 8)
- * are rejected with BUDE_ERR_ARG.  Calls share that array: calls whose work overlaps on one GPU
- * race and must be serialised by the caller.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) and should come before any stream capture.  Atom types
- * outside the forcefield give BUDE_ERR_TYPE and leave energies unwritten. */
+ * allowed.  Every pointer is a buffer in the current device's own memory (or managed memory):
+ * protein, ligand (16-byte aligned) and forcefield records, poses as six float fields at
+ * poses + k*pose_stride, and the output energies[nposes]; host memory and other GPUs' memory give
+ * BUDE_ERR_ARG.  `stream` is a cudaStream_t (NULL: the default stream); the call reads a status
+ * word back and returns after `stream` has drained, with the energies written.  The working
+ * memory (per-deck protein slab, pose transforms, irregular-pose bits, status words) is one fixed
+ * device array inside the library of about 11 MiB, held by every GPU that loads it until the
+ * process exits: sizes above BUDE_NOALLOC_MAX_POSES poses or BUDE_NOALLOC_MAX_SLAB_RECORDS slab
+ * records (forcefield types x protein atoms rounded up to 8) are rejected with BUDE_ERR_ARG.
+ * Calls share that array: calls whose work overlaps on one GPU race and must be serialised by the
+ * caller.  The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * and keeps it for the process: make that first call before any stream capture begins, and do not
+ * use the entry point on a device after cudaDeviceReset.  Atom types outside the forcefield give
+ * BUDE_ERR_TYPE and leave energies unwritten. */
 #define BUDE_NOALLOC_MAX_POSES 65536
 #define BUDE_NOALLOC_MAX_SLAB_RECORDS 131072
 int bude_gpu_fasten_noalloc(const bude_atom *protein, int32_t natpro, const bude_atom *ligand, int32_t natlig,

@@ -27,6 +27,13 @@ void release_batch(Context &c) {
   c.b_items.release();
   c.b_counter.release();
   c.b_partial.release();
+  c.b_edge_mask.release();
+  c.b_pose_off.release();
+  c.b_lig_off.release();
+  c.b_lig_all.release();
+  c.b_lig_any.release();
+  c.b_irregular_ligands = 0;
+  c.b_lig_all_host.clear();
   c.have_batch = false;
   c.items_ppb = 0;
   c.items_ppwi = 0;
@@ -82,13 +89,34 @@ int upload_batch(Context &c, const bude_atom *protein, int natpro, const bude_ff
   if (!rc) rc = c.b_xform.reserve((size_t)12 * np * sizeof(float), "batch transforms");
   if (!rc) rc = c.b_energies.reserve((size_t)np * sizeof(float), "batch energies");
   if (!rc) rc = c.b_counter.reserve(256, "batch work counter");
+  if (!rc) rc = c.b_edge_mask.reserve((size_t)(np + 31) / 32 * sizeof(unsigned), "batch irregular-pose bits");
+  if (!rc) rc = c.b_pose_off.reserve((size_t)(nligands + 1) * sizeof(long long), "batch pose offsets");
+  if (!rc) rc = c.b_lig_off.reserve((size_t)(nligands + 1) * sizeof(int), "batch atom offsets");
+  if (!rc) rc = c.b_lig_all.reserve((size_t)std::max(nligands, 1), "batch irregular ligands");
+  if (!rc) rc = c.b_lig_any.reserve(sizeof(int), "batch irregular ligand count");
   if (rc) return rc;
+  // Ligands outside the regular-deck bounds (edge_pose.cuh): all their poses go to edge_pose_kernel.
+  std::vector<unsigned char> lig_all((size_t)std::max(nligands, 1), 0);
+  int n_irregular = 0;
+  for (int l = 0; l < nligands; ++l) {
+    lig_all[(size_t)l] = !ligand_regular(c, atoms + lig_off[l], lig_off[l + 1] - lig_off[l], ff);
+    n_irregular += lig_all[(size_t)l];
+  }
   cudaError_t e = cudaSuccess;
   if (total_atoms > 0) e = copy_sync(c, c.b_ligands.ptr, atoms, (size_t)total_atoms * 16, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && total_poses > 0)
     e = copy2d_sync(c, c.b_poses.ptr, (size_t)total_poses * sizeof(float), poses, (size_t)pose_stride * sizeof(float),
                     (size_t)total_poses * sizeof(float), 6, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = copy_sync(c, c.b_pose_off.ptr, pose_off, (size_t)(nligands + 1) * sizeof(long long), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = copy_sync(c, c.b_lig_off.ptr, lig_off, (size_t)(nligands + 1) * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && nligands > 0)
+    e = copy_sync(c, c.b_lig_all.ptr, lig_all.data(), (size_t)nligands, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = copy_sync(c, c.b_lig_any.ptr, &n_irregular, sizeof(int), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_error(e, "batch upload");
+  c.b_irregular_ligands = n_irregular;
+  c.b_lig_all_host.assign(lig_all.begin(), lig_all.begin() + nligands);
   c.have_batch = true;
   ++c.batch_uploads;
   if (keep) return BUDE_OK;
@@ -242,11 +270,13 @@ static int enqueue_persistent(Context &c, const bude_launch_cfg &cfg, int grid, 
   if (c.batch_poses > 0) {
     const int tb = 256;
     pose_xform_kernel<<<(unsigned)((c.batch_poses + tb - 1) / tb), tb, 0, c.stream>>>(
-        c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>());
+        c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>(), c.b_edge_mask.as<unsigned>());
     c.launches++;
   }
-  return enqueue_items(c, cfg, grid, items, n_items, c.b_xform.as<float4>(), c.b_energies.as<float>(),
-                       c.b_partial.as<float>(), c.batch_poses);
+  int rc = enqueue_items(c, cfg, grid, items, n_items, c.b_xform.as<float4>(), c.b_energies.as<float>(),
+                         c.b_partial.as<float>(), c.batch_poses);
+  if (rc) return rc;
+  return enqueue_edge_batch(c, c.b_xform.as<float>(), c.b_energies.as<float>(), nullptr, c.stream);
 }
 
 static int persistent_grid(Context &c, const bude_launch_cfg &cfg, int *grid) {
@@ -313,7 +343,7 @@ int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand) {
     if (rc) return rc;
     cudaError_t e = cudaGraphLaunch(c.graph, c.stream);
     if (e != cudaSuccess) return cuda_error(e, "graph launch");
-    c.launches += (c.batch_poses > 0 ? 2 : 1) + (shape.split > 1 && c.n_items > 0 ? 1 : 0);
+    c.launches += (c.batch_poses > 0 ? 3 : 1) + (shape.split > 1 && c.n_items > 0 ? 1 : 0);
     return BUDE_OK;
   }
   // One plain exact-kernel launch per ligand, each with its own wave-model split (cluster
@@ -321,7 +351,7 @@ int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand) {
   if (c.batch_poses > 0) {
     const int tb = 256;
     pose_xform_kernel<<<(unsigned)((c.batch_poses + tb - 1) / tb), tb, 0, c.stream>>>(
-        c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>());
+        c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>(), c.b_edge_mask.as<unsigned>());
     c.launches++;
   }
   for (int l = 0; l < c.nligands; ++l) {
@@ -335,7 +365,7 @@ int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand) {
                             c.b_xform.as<float>() + c.pose_off[l] * 12, c.b_energies.as<float>() + c.pose_off[l], n);
     if (rc) return rc;
   }
-  return BUDE_OK;
+  return enqueue_edge_batch(c, c.b_xform.as<float>(), c.b_energies.as<float>(), nullptr, c.stream);
 }
 
 int autotune_batch(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms) {

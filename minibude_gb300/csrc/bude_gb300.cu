@@ -91,11 +91,85 @@ int ensure_slab(Context &c, const bude_atom *protein, int natpro, const bude_ffp
   std::vector<float> slab;
   build_slab(protein, natpro, ff, ntypes, c.natpro_pad, slab);
   int rc = c.slab.reserve(slab.size() * sizeof(float), "slab");
+  if (!rc) rc = c.raw_protein.reserve((size_t)std::max(natpro, 1) * sizeof(bude_atom), "protein records");
+  if (!rc) rc = c.raw_ff.reserve((size_t)ntypes * sizeof(bude_ffparams), "forcefield records");
   if (rc) return rc;
   cudaError_t e = copy_sync(c, c.slab.ptr, slab.data(), slab.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && natpro > 0)
+    e = copy_sync(c, c.raw_protein.ptr, protein, (size_t)natpro * sizeof(bude_atom), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = copy_sync(c, c.raw_ff.ptr, ff, (size_t)ntypes * sizeof(bude_ffparams), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_error(e, "slab upload");
+  c.host_ff.assign(ff, ff + ntypes);
+  // The protein's half of the regular-deck bounds (edge_pose.cuh); types were checked by the caller.
+  c.protein_regular = true;
+  c.protein_min_radius = FLT_MAX;
+  for (int j = 0; j < natpro; ++j) {
+    const bude_ffparams &f = ff[protein[j].type];
+    c.protein_regular = c.protein_regular && protein_atom_regular(protein[j]) && param_regular(f);
+    c.protein_min_radius = std::min(c.protein_min_radius, f.radius);
+  }
   c.slab_key = std::move(key);
   if (rebuilt) *rebuilt = true;
+  return BUDE_OK;
+}
+
+bool ligand_regular(const Context &c, const bude_atom *ligand, int natlig, const bude_ffparams *ff) {
+  if (natlig == 0 || c.natpro == 0) return true; // no pairs: every energy is 0, as in the reference
+  if (!c.protein_regular) return false;
+  float min_radius = FLT_MAX;
+  for (int i = 0; i < natlig; ++i) {
+    const bude_ffparams &f = ff[ligand[i].type];
+    if (!ligand_atom_regular(ligand[i].x, ligand[i].y, ligand[i].z) || !param_regular(f)) return false;
+    min_radius = std::min(min_radius, f.radius);
+  }
+  // FP32 addition is monotone, so this bounds every pair's radius sum (pair_record's radij).
+  const float min_sum = c.protein_min_radius + min_radius;
+  return min_sum >= kMinRadiusSum;
+}
+
+int enqueue_edge_single(Context &c, const float4 *ligand, int natlig, bool all, const unsigned *mask,
+                        const float *xform, float *energies, long long n, cudaStream_t st) {
+  if (n <= 0) return BUDE_OK;
+  EdgeArgs a{};
+  a.mask = mask;
+  a.all = all ? 1 : 0;
+  a.nposes = n;
+  a.nlig = 1;
+  a.ligand = ligand;
+  a.natlig = natlig;
+  a.protein = c.raw_protein.as<bude_atom>();
+  a.natpro = c.natpro;
+  a.ff = c.raw_ff.as<bude_ffparams>();
+  a.xform = xform;
+  a.energies = energies;
+  edge_pose_kernel<<<edge_grid(n, c.num_sms), 256, 0, st>>>(a);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "edge_pose_kernel launch");
+  c.launches++;
+  return BUDE_OK;
+}
+
+int enqueue_edge_batch(Context &c, const float *xform, float *energies, unsigned char *flag, cudaStream_t st) {
+  if (c.batch_poses <= 0) return BUDE_OK;
+  EdgeArgs a{};
+  a.mask = c.b_edge_mask.as<unsigned>();
+  a.nposes = c.batch_poses;
+  a.pose_off = c.b_pose_off.as<long long>();
+  a.lig_off = c.b_lig_off.as<int>();
+  a.lig_any = c.b_lig_any.as<int>();
+  a.lig_all = c.b_lig_all.as<unsigned char>();
+  a.nlig = c.nligands;
+  a.ligand = c.b_ligands.as<float4>();
+  a.protein = c.raw_protein.as<bude_atom>();
+  a.natpro = c.natpro;
+  a.ff = c.raw_ff.as<bude_ffparams>();
+  a.xform = xform;
+  a.energies = energies;
+  a.flag = flag;
+  edge_pose_kernel<<<edge_grid(c.batch_poses, c.num_sms), 256, 0, st>>>(a);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "edge_pose_kernel launch");
+  c.launches++;
   return BUDE_OK;
 }
 
@@ -223,14 +297,17 @@ int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid) {
     const int tb = 256;
     const long long nb = (c.nposes + tb - 1) / tb;
     pose_xform_kernel<<<(unsigned)nb, tb, 0, c.stream>>>(c.poses.as<float>(), c.pose_stride, c.nposes,
-                                                         c.xform.as<float4>());
+                                                         c.xform.as<float4>(), c.edge_mask.as<unsigned>());
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "pose_xform_kernel launch");
     c.launches++;
   }
   if (mid) cudaEventRecord(mid, c.stream);
-  return launch_exact_range(c, cfg, c.ligand.as<float4>(), c.natlig, c.xform.as<float>(), c.energies.as<float>(),
-                            c.nposes);
+  rc = launch_exact_range(c, cfg, c.ligand.as<float4>(), c.natlig, c.xform.as<float>(), c.energies.as<float>(),
+                          c.nposes);
+  if (rc) return rc;
+  return enqueue_edge_single(c, c.ligand.as<float4>(), c.natlig, c.deck_irregular, c.edge_mask.as<unsigned>(),
+                             c.xform.as<float>(), c.energies.as<float>(), c.nposes, c.stream);
 }
 
 // The exact kernel (and, for a global-reduce split, slice_reduce_kernel) over `nposes` poses whose
@@ -319,6 +396,7 @@ static int upload_ligand(Context &c, const bude_atom *ligand, int natlig) {
                        ligand[i].type, c.ntypes);
   int rc = c.ligand.reserve((size_t)std::max(natlig, 1) * 16, "ligand");
   if (rc) return rc;
+  c.deck_irregular = !ligand_regular(c, ligand, natlig, c.host_ff.data());
   if (natlig > 0) {
     // bude_atom is {x, y, z, int32 type}: the same 16 bytes as the kernel's float4 view.
     cudaError_t e = cudaMemcpyAsync(c.ligand.ptr, ligand, (size_t)natlig * 16, cudaMemcpyHostToDevice, c.stream);
@@ -335,6 +413,7 @@ static int upload_poses(Context &c, const float *poses, long long stride, long l
   int rc = c.poses.reserve((size_t)6 * n * sizeof(float), "poses");
   if (!rc) rc = c.xform.reserve((size_t)12 * n * sizeof(float), "transforms");
   if (!rc) rc = c.energies.reserve((size_t)n * sizeof(float), "energies");
+  if (!rc) rc = c.edge_mask.reserve((size_t)(n + 31) / 32 * sizeof(unsigned), "irregular-pose bits");
   if (rc) return rc;
   if (nposes > 0) {
     cudaError_t e = cudaMemcpy2DAsync(c.poses.ptr, (size_t)nposes * sizeof(float), poses, (size_t)stride * sizeof(float),
@@ -419,6 +498,9 @@ void destroy_context(Context *c) {
   c->err.release();
   c->flush.release();
   c->partial.release();
+  c->raw_protein.release();
+  c->raw_ff.release();
+  c->edge_mask.release();
   release_batch(*c);
   release_surrogate(*c);
   release_screen(*c);

@@ -38,6 +38,7 @@
 #include <cooperative_groups.h>
 #include <cstdint>
 
+#include "edge_pose.cuh"
 #include "exact_shape.h"
 #include "ptx.cuh"
 
@@ -63,18 +64,31 @@ struct ExactArgs {
 
 // Pose transforms: src/cuda/fasten.hpp:45-71 / serial/fasten.hpp:28-53, one thread per pose.
 // Output: three float4 rows per pose, {r00, r01, r02, tx}, {r10, r11, r12, ty}, {r20, r21, r22, tz}.
+// With edge_mask, bit (i & 31) of word i >> 5 is set when pose i is irregular (edge_pose.cuh), so
+// edge_pose_kernel rescores it afterwards; blockDim must be a multiple of 32.
 // (Internal linkage, like slice_reduce_kernel, so several translation units may include this file.)
 static __global__ void __launch_bounds__(256) pose_xform_kernel(const float *__restrict__ poses, long long pstride,
-                                                         long long nposes, float4 *__restrict__ xform) {
+                                                         long long nposes, float4 *__restrict__ xform,
+                                                         unsigned *__restrict__ edge_mask) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nposes) return;
-  float sx, cx, sy, cy, sz, cz;
-  sincosf(poses[i], &sx, &cx);
-  sincosf(poses[pstride + i], &sy, &cy);
-  sincosf(poses[2 * pstride + i], &sz, &cz);
-  xform[3 * i + 0] = make_float4(cy * cz, sx * sy * cz - cx * sz, cx * sy * cz + sx * sz, poses[3 * pstride + i]);
-  xform[3 * i + 1] = make_float4(cy * sz, sx * sy * sz + cx * cz, cx * sy * sz - sx * cz, poses[4 * pstride + i]);
-  xform[3 * i + 2] = make_float4(-sy, sx * cy, cx * cy, poses[5 * pstride + i]);
+  bool irregular = false;
+  if (i < nposes) {
+    float sx, cx, sy, cy, sz, cz;
+    sincosf(poses[i], &sx, &cx);
+    sincosf(poses[pstride + i], &sy, &cy);
+    sincosf(poses[2 * pstride + i], &sz, &cz);
+    const float4 r0 = make_float4(cy * cz, sx * sy * cz - cx * sz, cx * sy * cz + sx * sz, poses[3 * pstride + i]);
+    const float4 r1 = make_float4(cy * sz, sx * sy * sz + cx * cz, cx * sy * sz - sx * cz, poses[4 * pstride + i]);
+    const float4 r2 = make_float4(-sy, sx * cy, cx * cy, poses[5 * pstride + i]);
+    xform[3 * i + 0] = r0;
+    xform[3 * i + 1] = r1;
+    xform[3 * i + 2] = r2;
+    irregular = !pose_regular(r0, r1, r2);
+  }
+  if (edge_mask) {
+    const unsigned bits = __ballot_sync(0xffffffffu, irregular);
+    if ((threadIdx.x & 31) == 0 && i < nposes) edge_mask[i >> 5] = bits;
+  }
 }
 
 

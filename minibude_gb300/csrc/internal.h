@@ -56,6 +56,13 @@ struct Context {
   int natpro = 0, natpro_pad = 0, natlig = 0, ntypes = 0;
   long long nposes = 0, pose_stride = 0;
   DevBuf ligand, slab, poses, xform, energies, err, flush, partial;
+  // Irregular poses and decks (edge_pose.cuh): the raw protein and forcefield records, the
+  // transform pass's irregular-pose bits of the deck's poses, and whether the deck is irregular.
+  DevBuf raw_protein, raw_ff, edge_mask;
+  std::vector<bude_ffparams> host_ff; // the forcefield the slab was built from
+  bool protein_regular = true;      // every protein atom and its forcefield record within bounds
+  float protein_min_radius = 0.f;   // smallest radius of the protein's atom types
+  bool deck_irregular = false;      // the uploaded deck (protein + ligand) is scored by edge_pose_kernel
   int flush_gen = 0;
   long long launches = 0;
   // batch of ligands (bude_gpu_upload_batch); shares the protein slab with the deck fields above
@@ -66,6 +73,11 @@ struct Context {
   long long batch_poses = 0;
   DevBuf b_ligands, b_poses, b_xform, b_energies, b_items, b_counter;
   DevBuf b_partial; // split x batch_poses slice sums of a split batch evaluation (graph-owned)
+  // Irregular poses of the batch: transform-pass bits, device pose/atom offsets, and the ligands
+  // whose every pose goes to edge_pose_kernel (lig_all flags and their count, both on the device).
+  DevBuf b_edge_mask, b_pose_off, b_lig_off, b_lig_all, b_lig_any;
+  int b_irregular_ligands = 0;
+  std::vector<unsigned char> b_lig_all_host; // host copy of the lig_all flags
   int items_ppb = 0;  // poses per item the device item list was built for
   int items_ppwi = 0; // and poses per thread (the cut of a ligand's last block depends on it)
   int n_items = 0;
@@ -157,6 +169,14 @@ int default_cfg(const Context &c, int ppwi, int wgsize, bude_launch_cfg &cfg);
 int enqueue_eval(Context &c, const bude_launch_cfg &cfg, cudaEvent_t mid = nullptr);
 int launch_exact_range(Context &c, const bude_launch_cfg &cfg, const float4 *ligand, int natlig, const float *xform,
                        float *energies, long long nposes);
+// Whether a ligand of natlig atoms keeps the uploaded protein's deck regular (edge_pose.cuh).
+bool ligand_regular(const Context &c, const bude_atom *ligand, int natlig, const bude_ffparams *ff);
+// Enqueue edge_pose_kernel for the deck's single ligand over n poses (mask and transforms of
+// those poses; energies overwritten where irregular, or everywhere when `all`).
+int enqueue_edge_single(Context &c, const float4 *ligand, int natlig, bool all, const unsigned *mask,
+                        const float *xform, float *energies, long long n, cudaStream_t st);
+// Enqueue edge_pose_kernel over the uploaded batch's poses (flag: optional per-pose marks).
+int enqueue_edge_batch(Context &c, const float *xform, float *energies, unsigned char *flag, cudaStream_t st);
 int check_device_error(Context &c);
 int flush_l2(Context &c);
 int probe_kernel_arch(int device, int *cc);

@@ -13,17 +13,21 @@
 //   * its size is fixed at build time (BUDE_NOALLOC_MAX_POSES transforms and
 //     BUDE_NOALLOC_MAX_SLAB_RECORDS slab records, about 11 MiB), and every GPU that loads this
 //     module holds it until the process exits;
-//   * every call on a device shares it and it keeps the last call's contents: the error word is
-//     cleared at the start of each call, the slab and transforms are rewritten in full;
+//   * every call on a device shares it and it keeps the last call's contents: the error and check
+//     words are reset at the start of each call, the slab, transforms and irregular-pose bits are
+//     rewritten in full;
 //   * calls whose work overlaps on one GPU (two host threads, or two streams) race on it and
 //     must be serialised by the caller;
 //   * in host code the array's name is only a stand-in: its device address is looked up once per
 //     device with cudaGetSymbolAddress, with that device current, by the first call made on the
-//     device.  That first call should therefore come before any stream capture.
+//     device, and kept for the life of the process.  A cudaDeviceReset would leave that address
+//     stale, so the entry point must not be used on a device after it has been reset.
+// Each call reads its error word back and synchronises the stream before it returns.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdint>
+#include <cstring>
 #include <mutex>
 
 #include "exact_kernel.cuh"
@@ -36,13 +40,18 @@ namespace {
 constexpr size_t kNaErrBytes = 256;
 constexpr size_t kNaXformBytes = (size_t)BUDE_NOALLOC_MAX_POSES * 3 * sizeof(float4);
 constexpr size_t kNaSlabBytes = (size_t)BUDE_NOALLOC_MAX_SLAB_RECORDS * kRecF4 * sizeof(float4);
-constexpr size_t kNaScratchBytes = kNaErrBytes + kNaXformBytes + kNaSlabBytes;
+constexpr size_t kNaMaskBytes = (size_t)BUDE_NOALLOC_MAX_POSES / 32 * sizeof(unsigned);
+constexpr size_t kNaScratchBytes = kNaErrBytes + kNaXformBytes + kNaSlabBytes + kNaMaskBytes;
 
-// Error bits of the scratch error word (bit 0 is the exact kernel's bounded-wait timeout).
+// Words of the scratch's first 256 bytes: [0] error bits, [1] and [2] the smallest forcefield
+// radius of the protein's and of the ligand's atoms as order-preserving keys (atomicMin).
+// Error bits (bit 0 is the exact kernel's bounded-wait timeout):
 constexpr unsigned kNaErrProteinType = 2u;
 constexpr unsigned kNaErrLigandType = 4u;
+constexpr unsigned kNaIrregular = 8u; // an atom or forcefield record outside the regular-deck bounds
 
-// The working memory of bude_gpu_fasten_noalloc: [error word | pose transforms | protein slab].
+// The working memory of bude_gpu_fasten_noalloc:
+// [error and check words | pose transforms | protein slab | irregular-pose bits].
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaScratchBytes];
 
 constexpr int kNaMaxDevices = 64;
@@ -94,27 +103,55 @@ __global__ void __launch_bounds__(256) na_slab_kernel(const bude_atom *__restric
   }
 }
 
-// Ligand atom types must index the slab; the exact kernel reads them unchecked.
-__global__ void na_ligand_check_kernel(const bude_atom *__restrict__ ligand, int natlig, int ntypes, unsigned *err) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < natlig; i += gridDim.x * blockDim.x) {
-    const int t = ligand[i].type;
-    if (t < 0 || t >= ntypes) atomicOr(err, kNaErrLigandType);
+__device__ __forceinline__ unsigned radius_key(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u); // ascending float order as unsigned order
+}
+
+// Per atom: ligand atom types must index the slab (the exact kernel reads them unchecked), and
+// the atoms and their forcefield records are checked against the regular-deck bounds
+// (edge_pose.cuh); the smallest radii of both sides go to words [1] and [2].  Atoms with a type
+// outside the forcefield are only flagged.
+__global__ void na_deck_check_kernel(const bude_atom *__restrict__ protein, int natpro,
+                                     const bude_atom *__restrict__ ligand, int natlig,
+                                     const bude_ffparams *__restrict__ ff, int ntypes, unsigned *words) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < natpro + natlig; i += gridDim.x * blockDim.x) {
+    const bool is_lig = i >= natpro;
+    const bude_atom a = is_lig ? ligand[i - natpro] : protein[i];
+    if (a.type < 0 || a.type >= ntypes) {
+      if (is_lig) atomicOr(&words[0], kNaErrLigandType); // protein types: na_slab_kernel
+      continue;
+    }
+    const bude_ffparams f = ff[a.type];
+    const bool ok = param_regular(f) && (is_lig ? ligand_atom_regular(a.x, a.y, a.z) : protein_atom_regular(a));
+    if (!ok) atomicOr(&words[0], kNaIrregular);
+    atomicMin(&words[is_lig ? 2 : 1], radius_key(f.radius));
   }
 }
 
-int na_read_error(unsigned *word, cudaStream_t st, unsigned *out) {
-  cudaError_t e = cudaMemcpyAsync(out, word, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+float key_radius(unsigned k) {
+  const unsigned u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+  float f;
+  std::memcpy(&f, &u, sizeof f);
+  return f;
+}
+
+// Read n words from the device into a caller-provided host array (no allocation) and wait.
+int na_read_words(const unsigned *words, int n, cudaStream_t st, unsigned *out) {
+  cudaError_t e = cudaMemcpyAsync(out, words, (size_t)n * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return e == cudaSuccess ? BUDE_OK : cuda_error(e, "no-alloc error word");
 }
 
-bool is_device_memory(const void *p) {
+// Device memory of `device` (the current device), or managed memory.  Another GPU's memory is
+// refused: the kernels would read it over the interconnect or fault when peer access is off.
+bool is_device_memory(const void *p, int device) {
   cudaPointerAttributes at{};
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  return (at.type == cudaMemoryTypeDevice && at.device == device) || at.type == cudaMemoryTypeManaged;
 }
 
 } // namespace
@@ -144,44 +181,54 @@ extern "C" int bude_gpu_fasten_noalloc(const bude_atom *protein, int32_t natpro,
     return set_error(BUDE_ERR_ARG, "NULL input or output buffer");
   if (reinterpret_cast<uintptr_t>(ligand) % 16 != 0)
     return set_error(BUDE_ERR_ARG, "ligand must be 16-byte aligned");
-  if (!is_device_memory(forcefield) || !is_device_memory(poses) || !is_device_memory(energies) ||
-      (natpro > 0 && !is_device_memory(protein)) || (natlig > 0 && !is_device_memory(ligand)))
-    return set_error(BUDE_ERR_ARG, "no-alloc entry point takes device buffers only");
-
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  if (!is_device_memory(forcefield, device) || !is_device_memory(poses, device) ||
+      !is_device_memory(energies, device) || (natpro > 0 && !is_device_memory(protein, device)) ||
+      (natlig > 0 && !is_device_memory(ligand, device)))
+    return set_error(BUDE_ERR_ARG, "no-alloc entry point takes buffers in the current device's memory only "
+                                   "(device %d)", device);
+
   unsigned char *scratch = nullptr;
   int rc = na_scratch(device, &scratch);
   if (rc) return rc;
   unsigned *err = reinterpret_cast<unsigned *>(scratch);
   float4 *xform = reinterpret_cast<float4 *>(scratch + kNaErrBytes);
   float4 *slab = reinterpret_cast<float4 *>(scratch + kNaErrBytes + kNaXformBytes);
+  unsigned *mask = reinterpret_cast<unsigned *>(scratch + kNaErrBytes + kNaXformBytes + kNaSlabBytes);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
 
-  // 1. clear the error word; slab and ligand check.
+  // 1. reset the error word and the two radius minima; slab and deck checks.
   e = cudaMemsetAsync(err, 0, sizeof(unsigned), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(err + 1, 0xff, 2 * sizeof(unsigned), st);
   if (e != cudaSuccess) return cuda_error(e, "no-alloc error word clear");
   {
     const long long n = (long long)ntypes * natpro_pad;
     const int blocks = (int)std::min<long long>((n + 255) / 256, 8LL * std::max(sms, 1));
     na_slab_kernel<<<blocks, 256, 0, st>>>(protein, natpro, forcefield, ntypes, natpro_pad, slab, err);
-    if (natlig > 0) na_ligand_check_kernel<<<(natlig + 255) / 256, 256, 0, st>>>(ligand, natlig, ntypes, err);
+    if (natpro + natlig > 0)
+      na_deck_check_kernel<<<(unsigned)std::min((natpro + natlig + 255) / 256, 4 * std::max(sms, 1)), 256, 0, st>>>(
+          protein, natpro, ligand, natlig, forcefield, ntypes, err);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "no-alloc slab launch");
   }
-  unsigned h = 0;
-  rc = na_read_error(err, st, &h);
+  unsigned h[3] = {0, 0, 0};
+  rc = na_read_words(err, 3, st, h);
   if (rc) return rc;
-  if (h & (kNaErrProteinType | kNaErrLigandType))
+  if (h[0] & (kNaErrProteinType | kNaErrLigandType))
     return set_error(BUDE_ERR_TYPE, "%s atom type outside the forcefield (%d types)",
-                     (h & kNaErrLigandType) ? "a ligand" : "a protein", ntypes);
+                     (h[0] & kNaErrLigandType) ? "a ligand" : "a protein", ntypes);
+  // The deck is irregular when an atom or record is out of bounds or the smallest FP32 radius sum
+  // is below the bound (FP32 addition is monotone); with no ligand-protein pair every energy is 0.
+  const float min_sum = key_radius(h[1]) + key_radius(h[2]);
+  const bool irregular = natpro > 0 && natlig > 0 && ((h[0] & kNaIrregular) || !(min_sum >= kMinRadiusSum));
 
   // 2. pose transforms and the exact kernel; protein slices (if any) are summed in a cluster, so
   //    no slice buffer is needed.
-  pose_xform_kernel<<<(unsigned)((nposes + 255) / 256), 256, 0, st>>>(poses, pose_stride, nposes, xform);
+  pose_xform_kernel<<<(unsigned)((nposes + 255) / 256), 256, 0, st>>>(poses, pose_stride, nposes, xform, mask);
   constexpr int P = 8, U = 2, W = 128, T = 64;
   const long long blocks = (nposes + (long long)P * W - 1) / ((long long)P * W);
   int split = 1;
@@ -218,8 +265,24 @@ extern "C" int bude_gpu_fasten_noalloc(const bude_atom *protein, int32_t natpro,
     e = cudaLaunchKernelEx(&lc, exact_kernel<P, U>, a);
   }
   if (e != cudaSuccess) return cuda_error(e, "no-alloc exact_kernel launch");
-  rc = na_read_error(err, st, &h);
+  // 3. irregular poses (or every pose of an irregular deck) by the reference's arithmetic.
+  EdgeArgs ea{};
+  ea.mask = mask;
+  ea.all = irregular ? 1 : 0;
+  ea.nposes = nposes;
+  ea.nlig = 1;
+  ea.ligand = reinterpret_cast<const float4 *>(ligand);
+  ea.natlig = natlig;
+  ea.protein = protein;
+  ea.natpro = natpro;
+  ea.ff = forcefield;
+  ea.xform = reinterpret_cast<const float *>(xform);
+  ea.energies = energies;
+  edge_pose_kernel<<<edge_grid(nposes, sms), 256, 0, st>>>(ea);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "no-alloc edge_pose_kernel launch");
+  rc = na_read_words(err, 1, st, h);
   if (rc) return rc;
-  if (h & 1u) return set_error(BUDE_ERR_TIMEOUT, "a bounded device wait ran out; energies are invalid");
+  if (h[0] & 1u) return set_error(BUDE_ERR_TIMEOUT, "a bounded device wait ran out; energies are invalid");
   return BUDE_OK;
 }

@@ -539,6 +539,10 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
         s.pose_off.as<long long>(), s.fb.as<int>(), c.b_energies.as<float>(), s.final_e.as<float>(),
         s.rescored.as<unsigned char>());
   }
+  // Irregular poses (edge_pose.cuh) get the reference's arithmetic in the final list, flagged as
+  // rescored, whatever the surrogate made of them.
+  rc = enqueue_edge_batch(c, c.b_xform.as<float>(), s.final_e.as<float>(), s.rescored.as<unsigned char>(), c.stream);
+  if (rc) return rc;
   cudaEventRecord(ev[4], c.stream);
   e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return cuda_error(e, "screen");

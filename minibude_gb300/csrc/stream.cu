@@ -19,7 +19,7 @@ namespace bude {
 
 struct StreamState {
   cudaStream_t h2d = nullptr, d2h = nullptr;
-  DevBuf poses[2], energies[2], xform;
+  DevBuf poses[2], energies[2], xform, edge_mask;
   cudaEvent_t copied[2] = {}, consumed[2] = {}, computed[2] = {}, returned[2] = {};
 };
 
@@ -35,6 +35,7 @@ void release_streamer(Context &c) {
       if (ev) cudaEventDestroy(ev);
   }
   s.xform.release();
+  s.edge_mask.release();
   if (s.h2d) cudaStreamDestroy(s.h2d);
   if (s.d2h) cudaStreamDestroy(s.d2h);
   delete c.streamer;
@@ -63,6 +64,7 @@ static int streamer(Context &c, long long chunk, StreamState **out) {
     if (!rc) rc = s.energies[b].reserve((size_t)chunk * sizeof(float), "streamed energies");
   }
   if (!rc) rc = s.xform.reserve((size_t)chunk * 12 * sizeof(float), "streamed transforms");
+  if (!rc) rc = s.edge_mask.reserve((size_t)(chunk + 31) / 32 * sizeof(unsigned), "streamed irregular-pose bits");
   if (rc) return rc;
   *out = &s;
   return BUDE_OK;
@@ -104,11 +106,15 @@ static int score_stream(Context &c, const bude_launch_cfg &cfg, const float *pos
     if (i >= 2) cudaStreamWaitEvent(c.stream, s.returned[b], 0); // energies slot copied back
     const int tb = 256;
     pose_xform_kernel<<<(unsigned)((n + tb - 1) / tb), tb, 0, c.stream>>>(s.poses[b].as<float>(), n, n,
-                                                                          s.xform.as<float4>());
+                                                                          s.xform.as<float4>(),
+                                                                          s.edge_mask.as<unsigned>());
     c.launches++;
     e = cudaEventRecord(s.consumed[b], c.stream);
     if (e != cudaSuccess) break;
     rc = launch_exact_range(c, cfg, c.ligand.as<float4>(), c.natlig, s.xform.as<float>(), s.energies[b].as<float>(), n);
+    if (!rc)
+      rc = enqueue_edge_single(c, c.ligand.as<float4>(), c.natlig, c.deck_irregular, s.edge_mask.as<unsigned>(),
+                               s.xform.as<float>(), s.energies[b].as<float>(), n, c.stream);
     if (rc) break;
     e = cudaEventRecord(s.computed[b], c.stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s.d2h, s.computed[b], 0);

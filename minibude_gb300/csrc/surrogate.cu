@@ -446,7 +446,7 @@ static int batch_transforms(Context &c) {
   if (c.batch_poses == 0) return BUDE_OK;
   const int tb = 256;
   pose_xform_kernel<<<(unsigned)((c.batch_poses + tb - 1) / tb), tb, 0, c.stream>>>(
-      c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>());
+      c.b_poses.as<float>(), c.batch_poses, c.batch_poses, c.b_xform.as<float4>(), c.b_edge_mask.as<unsigned>());
   c.launches++;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? BUDE_OK : cuda_error(e, "pose transforms");
@@ -486,13 +486,26 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
   rc = upload_pose_ligands(c, s, lig_n);
   if (!rc) rc = batch_transforms(c);
   if (rc) return rc;
+  // The poses learnt from: regular ones (edge_pose.cuh: finite transforms, translations and atoms
+  // within bounds) with finite labels.  Every pose of an ordinary batch qualifies.
+  std::vector<float> hl((size_t)np);
+  std::vector<unsigned> edge((size_t)(np + 31) / 32);
+  cudaError_t e = copy_sync(c, hl.data(), s.labels.ptr, (size_t)np * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = copy_sync(c, edge.data(), c.b_edge_mask.ptr, edge.size() * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "labels read-back");
+  std::vector<int> order, rowoff;
+  order.reserve((size_t)np);
+  for (int l = 0; l < c.nligands; ++l) {
+    if (c.b_lig_all_host[(size_t)l]) continue;
+    for (long long p = c.pose_off[l]; p < c.pose_off[l + 1]; ++p)
+      if (!((edge[(size_t)(p >> 5)] >> (p & 31)) & 1u) && std::isfinite(hl[(size_t)p])) order.push_back((int)p);
+  }
+  const long long n_used = (long long)order.size();
+  if (n_used == 0) return set_error(BUDE_ERR_ARG, "the batch has no regular pose with a finite label to train on");
   // b4 starts at the mean label per ligand atom.
   if (s.step == 0) {
-    std::vector<float> hl((size_t)np);
-    cudaError_t e = copy_sync(c, hl.data(), s.labels.ptr, (size_t)np * 4, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_error(e, "labels read-back");
     double sl = 0, sa = 0;
-    for (long long p = 0; p < np; ++p) {
+    for (int p : order) {
       sl += std::asinh(hl[(size_t)p] / kLossScale) * kLossScale;
       sa += lig_n[(size_t)p];
     }
@@ -500,11 +513,9 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
     e = copy_sync(c, s.params.as<float>() + kOffB4, &b4, sizeof b4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_error(e, "output bias");
   }
-  const int nb_full = (int)std::min<long long>(batch, np);
-  const int steps_per_epoch = (int)((np + nb_full - 1) / nb_full);
+  const int nb_full = (int)std::min<long long>(batch, n_used);
+  const int steps_per_epoch = (int)((n_used + nb_full - 1) / nb_full);
   const long long total_steps = (long long)epochs * steps_per_epoch;
-  std::vector<int> order((size_t)np), rowoff;
-  std::iota(order.begin(), order.end(), 0);
   std::mt19937_64 rng(seed);
   rc = s.epoch_pose.reserve((size_t)np * 4, "epoch poses");
   if (!rc) rc = s.epoch_rowoff.reserve((size_t)(np + steps_per_epoch) * 4, "epoch row offsets");
@@ -521,7 +532,7 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
     rowoff.clear();
     std::vector<long long> rows_of(steps_per_epoch);
     for (int st = 0; st < steps_per_epoch; ++st) {
-      const long long a = (long long)st * nb_full, b = std::min(np, a + nb_full);
+      const long long a = (long long)st * nb_full, b = std::min(n_used, a + nb_full);
       int r = 0;
       for (long long i = a; i < b; ++i) {
         rowoff.push_back(r);
@@ -530,13 +541,13 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
       rowoff.push_back(r);
       rows_of[st] = r;
     }
-    cudaMemcpyAsync(s.epoch_pose.ptr, order.data(), (size_t)np * 4, cudaMemcpyHostToDevice, c.stream);
+    cudaMemcpyAsync(s.epoch_pose.ptr, order.data(), (size_t)n_used * 4, cudaMemcpyHostToDevice, c.stream);
     cudaMemcpyAsync(s.epoch_rowoff.ptr, rowoff.data(), rowoff.size() * 4, cudaMemcpyHostToDevice, c.stream);
     cudaStreamSynchronize(c.stream); // the host vectors are rewritten next epoch
     double loss_sum = 0;
     long long ro = 0;
     for (int st = 0; st < steps_per_epoch && !rc; ++st) {
-      const long long a = (long long)st * nb_full, b = std::min(np, a + nb_full);
+      const long long a = (long long)st * nb_full, b = std::min(n_used, a + nb_full);
       const int nb = (int)(b - a);
       // Cosine decay from lr to lr / 20 over the run.
       const double frac = total_steps > 1 ? (double)done / (double)(total_steps - 1) : 0.0;
@@ -552,10 +563,10 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
         for (float v : lh) loss_sum += v;
       }
     }
-    last_loss = loss_sum / (double)np;
+    last_loss = loss_sum / (double)n_used;
   }
   cudaEventRecord(e1, c.stream);
-  cudaError_t e = cudaStreamSynchronize(c.stream);
+  e = cudaStreamSynchronize(c.stream);
   if (!rc && e != cudaSuccess) rc = cuda_error(e, "surrogate training");
   if (!rc && train_ms) cudaEventElapsedTime(train_ms, e0, e1);
   cudaEventDestroy(e0);

@@ -87,3 +87,15 @@ def test_flop_counts(ppwi):
     setup = (n / ppwi) * (2.0 * lig + 10.0 * lig * pro)
     assert ref == pytest.approx(algorithmic_flops(n, lig, pro) + setup, rel=1e-12)
     assert reference_formula_flops(n, lig, pro, 2 * ppwi) < ref
+
+
+def test_oracle_nonfinite_poses_match_the_reference_serial_model():
+    # NaN and infinite poses, overflowing squared distances, far and huge-angle poses: the oracle
+    # gives NaN exactly where the reference's SerialBude<1> does and its energies elsewhere.
+    deck, refs, f64 = load_golden("nonfinite")
+    e = oracle.fasten_f32(deck)
+    nan = np.isnan(refs)
+    assert nan.sum() == 13
+    assert np.array_equal(np.isnan(e), nan)
+    max_diff, failed = validate(e[~nan], refs[~nan])
+    assert failed == [] and max_diff < 0.025, (max_diff, failed[:5])
