@@ -15,6 +15,13 @@ Printed (one JSON line, rank 0):
              28 per pose, src/main.cpp:359)
   cpu_baseline  the oracle's FP32 restatement of the reference kernel (OpenMP, -O3 -ffast-math as
              the reference's release build) on a bounded sample of the same deck, all host cores
+  parity     the timed launch's energies against the reference's own energies for the deck's first
+             256 poses (committed golden fixture) and against the CPU baseline's energies for its
+             sample: max_diff_% by the reference's validation rule (src/main.cpp:329-342)
+  batch, screen  (one GPU, default workload) the second half of the headline metric: batched
+             ragged scoring of 256 ligands, and surrogate-screened scoring of 1,024 ligands x 16,384
+             poses next to batched exhaustive exact scoring of the same ligands, each with its own
+             clocks, roofline and recall figures
 
 `--impl reference` times that CPU implementation alone, as the reference arm.
 Under torchrun each rank runs its own deck (seed = rank) on its own GPU: weak scaling, no
@@ -70,6 +77,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="default workload: skip the batch and screen sub-records")
     return ap.parse_args()
 
 
@@ -187,7 +196,8 @@ def traffic_per_launch(nposes: int, kernel: str = "exact_kernel"):
 
 
 def cpu_sample_run(deck, seconds: float, fast: bool = True):
-    """Time the oracle on the first S poses of `deck`, S sized for about `seconds` of work."""
+    """Time the oracle on the first S poses of `deck`, S sized for about `seconds` of work; returns
+    the cpu_baseline record and the energies it computed (the checker of the GPU's energies)."""
     import oracle
     nthreads = os.cpu_count() or 1
     probe = deck.head(min(deck.nposes, 256))
@@ -198,11 +208,32 @@ def cpu_sample_run(deck, seconds: float, fast: bool = True):
     n = max(256, n // 256 * 256)
     sample = deck.head(n)
     t = time.perf_counter()
-    oracle.fasten_f32(sample, nthreads=nthreads, fast=fast)
+    energies = oracle.fasten_f32(sample, nthreads=nthreads, fast=fast)
     dt = time.perf_counter() - t
-    return {"value": sample.interactions / dt / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"first {n} of {deck.nposes} poses of the same deck ({sample.interactions:.3e} interactions, "
-                      f"{dt:.1f} s); oracle/bude_oracle.c built -O3 -ffast-math -fopenmp"}
+    return ({"value": sample.interactions / dt / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
+             "sample": f"first {n} of {deck.nposes} poses of the same deck ({sample.interactions:.3e} interactions, "
+                       f"{dt:.1f} s); oracle/bude_oracle.c built -O3 -ffast-math -fopenmp"}, energies)
+
+
+def golden_head(spec, seed: int):
+    """(name, energies) of the committed fixture holding the first poses of this synthetic deck with
+    the reference's own energies (OmpBude<16>), or None."""
+    if seed != 0:
+        return None
+    name = {"synthetic-4096x64x1048576": "large_head", "synthetic-938x26x65536": "small_head"}.get(spec.name)
+    path = os.path.join(ROOT, "tests", "golden", name or "-", "ref_energies.f32")
+    if not name or not os.path.exists(path):
+        return None
+    return name, np.fromfile(path, "<f4")
+
+
+def parity_record(got, want, what: str) -> dict:
+    """The reference's validation (src/main.cpp:329-342) of `got` against `want`."""
+    from minibude_gb300 import validate
+    from minibude_gb300.validate import validate_abs
+    max_diff, failed = validate(got, want)
+    return {"against": what, "poses": int(len(want)), "max_diff_pct": round(float(max_diff), 6),
+            "max_diff_abs_pct": round(float(validate_abs(got, want)), 6), "failed": len(failed)}
 
 
 def parse_cfg(ctx, text: str, deck):
@@ -254,6 +285,7 @@ def run_ours(args, dist: Dist):
         dist.barrier()
     launches = ctx.launch_count() - launches0
     clk = clocks.summary(peaks.get("sm_max_mhz", 2070.0))
+    energies = ctx.download()  # the last timed evaluation's, checked below
     step_ms = float(np.mean(ms))
     step_ms_max = dist.max(step_ms)
     interactions = deck.interactions
@@ -322,8 +354,17 @@ def run_ours(args, dist: Dist):
         pin_e.free()
     ctx.close()
 
+    parity = []
+    gold = golden_head(spec, dist.rank) if args.workload in ("large", "small") and not args.nposes else None
+    if gold:
+        parity.append(parity_record(energies[:len(gold[1])], gold[1],
+                                    f"the reference's OmpBude<16> energies (tests/golden/{gold[0]})"))
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_sample_run(deck, args.cpu_seconds)
+        out["cpu_baseline"], cpu_e = cpu_sample_run(deck, args.cpu_seconds)
+        parity.append(parity_record(energies[:len(cpu_e)], cpu_e, "the CPU baseline's energies of its sample"))
+    if parity:
+        out["parity_max_diff_pct"] = max(p["max_diff_pct"] for p in parity)
+        out["parity"] = parity
     return out
 
 
@@ -572,11 +613,21 @@ def run_screen(args, dist: Dist):
     launches = ctx.launch_count() - launches0
     clk = clocks.summary(peaks.get("sm_max_mhz", 2070.0))
     final, rescored, err = ctx.screen_download(screen.nligands)
+    sur = ctx.surrogate_download()  # the surrogate's energies of every pose (the last screen's)
     step = dist.max(float(np.mean([st["total_ms"] for st in stats])))
     off = screen.pose_offsets()
     r100 = _recall_top(exact, final, off, topn=100, budget=100)
     r1in = _recall_top(exact, final, off, frac=0.01, rescored=rescored)
     last = stats[-1]
+    # The audit sample: the rescored poses that are not picks (a ligand's ceil(0.02 n) lowest
+    # surrogate energies, ties in pose order).  Its relative energy error sits beside the rank
+    # measure the audit acts on.
+    audit = rescored.copy()
+    for l in range(screen.nligands):
+        a, b = off[l], off[l + 1]
+        k = int(np.ceil(np.float32(0.02) * np.float32(b - a)))
+        audit[a + np.argsort(sur[a:b], kind="stable")[:k]] = False
+    rel = np.abs(sur[audit].astype(np.float64) - exact[audit]) / np.maximum(np.abs(exact[audit]), 1.0)
     out = {"metric": "screened poses/s", "value": round(dist.world * screen.total_poses / (step * 1e-3), 1),
            "unit": "poses/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": round(step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -593,8 +644,22 @@ def run_screen(args, dist: Dist):
                       "surrogate_ms": round(last["surrogate_ms"], 3), "rescore_ms": round(last["rescore_ms"], 3),
                       "fallback_ms": round(last["fallback_ms"], 3), "rescored_poses": int(last["rescored_poses"]),
                       "fallback_ligands": int(last["fallback_ligands"]),
-                      "max_audit_error": round(float(last["max_audit_error"]), 4), "exact_launch": cfg.as_dict(),
-                      "screen_exact_launch": scfg.as_dict()},
+                      "max_audit_error": round(float(last["max_audit_error"]), 4),
+                      "audit_error_definition": "1 - Spearman rank correlation of surrogate and exact energies "
+                                                "over a ligand's audit poses (at most 2048); a ligand falls back to "
+                                                "exhaustive exact scoring above audit_tol (the 5% of the workload "
+                                                "text, read as a rank error: a pre-screen only has to order poses)",
+                      "audit_energy_error": {"poses": int(audit.sum()),
+                                             "median_rel": round(float(np.median(rel)), 4) if rel.size else None,
+                                             "p90_rel": round(float(np.percentile(rel, 90)), 4) if rel.size else None,
+                                             "definition": "|surrogate - exact| / max(|exact|, 1) on the audit "
+                                                           "sample"},
+                      "surrogate_model": "per (pose, ligand atom) row: 16-wide type embedding + transformed xyz "
+                                         "+ 13 protein-field channels sampled from a trilinear grid (in place of "
+                                         "nearest-protein-tile distances) = 32 features; 3 hidden layers of 128 "
+                                         "with hard-swish (the piecewise-polynomial SiLU: no MUFU on the "
+                                         "critical path); BF16 weights, FP32 accumulation; summed per pose",
+                      "exact_launch": cfg.as_dict(), "screen_exact_launch": scfg.as_dict()},
            "gpu_launches": launches, "clocks": clk}
     # dominant kernel: the surrogate scorer over every pose
     rows = sum(len(l) * p.shape[1] for l, p in zip(screen.ligands, screen.poses))
@@ -668,6 +733,12 @@ def main():
             out = run_screen(args, dist)
         else:
             out = run_ours(args, dist)
+            if args.workload == "large" and dist.world == 1 and not args.no_sub:
+                # The second half of the headline metric, on the same GPU after the exact line.
+                sub = argparse.Namespace(**vars(args))
+                sub.steps, sub.cfg, sub.batch_ligands = max(3, min(args.steps, 10)), "auto", 0
+                out["batch"] = run_batch(sub, dist)
+                out["screen"] = run_screen(sub, dist)
         if dist.rank == 0:
             print(json.dumps(out), flush=True)
     finally:
