@@ -57,13 +57,15 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["large", "small", "bm2_long", "batch", "surrogate", "screen"],
+    ap.add_argument("--workload", choices=["large", "small", "bm2_long", "batch", "surrogate", "screen", "sweep"],
                     default="large",
                     help="large: 4096 x 64 x 1M-pose deck (default); small: bm1-sized deck; batch: 256 ligands "
                          "(12-96 atoms, 4096-65536 poses each) against the 2672-atom bm2 protein; surrogate: train on "
                          "2M poses of 512 ligands (938-atom protein), score 64 held-out ligands x 65536 poses; screen: "
                          "1024 ligands (16-80 atoms) x 16384 poses against the bm2 protein, surrogate-screened vs "
-                         "batched exhaustive exact")
+                         "batched exhaustive exact; sweep: the reference driver's PPWI x wgsize sweep on the "
+                         "4096 x 64 x 1M deck, each shape with the wave model's protein split, against the "
+                         "autotuner's pick")
     ap.add_argument("--epochs", type=int, default=80, help="surrogate training epochs (surrogate/screen workloads)")
     ap.add_argument("--grid-spacing", type=float, default=1.25,
                     help="spacing in A of the surrogate's protein-field grid (surrogate/screen workloads)")
@@ -360,10 +362,24 @@ def run_ours(args, dist: Dist):
         parity.append(parity_record(energies[:len(gold[1])], gold[1],
                                     f"the reference's OmpBude<16> energies (tests/golden/{gold[0]})"))
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        import oracle
         out["cpu_baseline"], cpu_e = cpu_sample_run(deck, args.cpu_seconds)
-        parity.append(parity_record(energies[:len(cpu_e)], cpu_e, "the CPU baseline's energies of its sample"))
+        rec = parity_record(energies[:len(cpu_e)], cpu_e, "the CPU baseline's energies of its sample (two FP32 "
+                                                           "evaluations: the rule also counts their rounding)")
+        # Both FP32 results against an FP64 rerun of the reference kernel on the first poses: the GPU's
+        # error next to the reference arithmetic's own (the CPU baseline is that arithmetic at the
+        # reference's release flags).
+        k = min(len(cpu_e), 16384)
+        f64 = oracle.fasten_f64(deck.head(k), nthreads=os.cpu_count() or 1)
+        scale = np.maximum(np.abs(f64), 1.0)
+        rec["fp64_check"] = {"poses": k,
+                             "gpu_max_rel_err": float("%.3g" % np.max(np.abs(energies[:k] - f64) / scale)),
+                             "cpu_max_rel_err": float("%.3g" % np.max(np.abs(cpu_e[:k] - f64) / scale)),
+                             "definition": "|E - E_fp64| / max(|E_fp64|, 1)"}
+        parity.append(rec)
     if parity:
-        out["parity_max_diff_pct"] = max(p["max_diff_pct"] for p in parity)
+        # The headline figure: the reference's own check against the reference's own energies.
+        out["parity_max_diff_pct"] = parity[0]["max_diff_pct"]
         out["parity"] = parity
     return out
 
@@ -675,6 +691,54 @@ def run_screen(args, dist: Dist):
     return out
 
 
+def run_sweep(args, dist: Dist):
+    """The reference driver's brute-force search (src/main.cpp:517-541: every PPWI x wgsize) on the
+    4096 x 64 x 1M deck, each (PPWI, wgsize) with the wave model's protein split in both reduction
+    modes and unsplit, timed like the headline (L2 flushed, CUDA events); the autotuner's pick is
+    timed the same way.  PPWI 32, 64 and 128 run as 16 poses per thread (the register bound)."""
+    from minibude_gb300 import build
+    from minibude_gb300.model import GpuContext, launch_cfg
+    build.build_library()
+    deck = synthetic_deck(LARGE, seed=dist.rank, nposes=args.nposes or None)
+    ctx = GpuContext(dist.local_rank)
+    ctx.upload(deck)
+    reps = max(2, min(args.steps, 5))
+
+    def timed(cfg):
+        ctx.run_many(cfg, 1, flush_l2=True)
+        ms, _ = ctx.run_many(cfg, reps, flush_l2=True)
+        return float(np.mean(ms))
+    t0 = time.perf_counter()
+    pick, predicted = ctx.autotune()
+    tune_s = time.perf_counter() - t0
+    rows = []
+    for p in (1, 2, 4, 8, 16):
+        for w in (64, 128, 256, 512):
+            base = ctx.default_cfg(p, w)  # wave-model split, global reduction
+            shapes = {(base.split, 0)}
+            if base.split > 1:
+                shapes.add((1, 0))
+                if base.split <= 8:
+                    shapes.add((base.split, 1))
+            for split, cl in sorted(shapes):
+                cfg = launch_cfg(p, w, split, base.tile, base.unroll, cluster=cl)
+                rows.append({"ppwi": p, "wgsize": w, "split": split, "cluster": cl, "unroll": base.unroll,
+                             "ms": round(timed(cfg), 4)})
+    pick_ms = timed(pick)
+    best = min(rows, key=lambda r: r["ms"])
+    ctx.close()
+    inter = deck.interactions
+    return {"metric": "exact GInteractions/s (autotuner pick)", "value": round(inter / (pick_ms * 1e-3) / 1e9, 3),
+            "unit": UNIT, "n_gpus": 1, "steps": reps, "warmup": 1, "ms_per_step": round(pick_ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded; the 4096-atom workload)",
+            "config": {"workload": LARGE.name, "l2": "flushed before every timed step (512 MB memset)"},
+            "autotuner": {"pick": pick.as_dict(), "ms": round(pick_ms, 4), "predicted_ms": round(predicted, 4),
+                          "tuning_s": round(tune_s, 3)},
+            "sweep_best": best, "sweep_best_gi_s": round(inter / (best["ms"] * 1e-3) / 1e9, 3),
+            "gap_pct": round(100.0 * (pick_ms - best["ms"]) / best["ms"], 3), "shapes": len(rows), "sweep": rows}
+
+
 def run_reference(args, dist: Dist):
     """The reference arm: the reference's CPU implementation of the path on the host cores."""
     import oracle
@@ -731,6 +795,8 @@ def main():
             out = run_surrogate(args, dist)
         elif args.workload == "screen":
             out = run_screen(args, dist)
+        elif args.workload == "sweep":
+            out = run_sweep(args, dist)
         else:
             out = run_ours(args, dist)
             if args.workload == "large" and dist.world == 1 and not args.no_sub:

@@ -409,9 +409,10 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   if (lr > 0.f) {
     s.step++;
     const float b1 = 0.9f, b2 = 0.999f;
-    const float lr_t = lr * std::sqrt(1.f - std::pow(b2, (float)s.step)) / (1.f - std::pow(b1, (float)s.step));
+    const double bc1 = 1.0 - std::pow((double)b1, (double)s.step), bc2 = 1.0 - std::pow((double)b2, (double)s.step);
     adam_kernel<<<(unsigned)((kNParams + 255) / 256), 256, 0, c.stream>>>(
-        s.params.as<float>(), s.adam_m.as<float>(), s.adam_v.as<float>(), gr, kNParams, lr_t, b1, b2, 1e-8f);
+        s.params.as<float>(), s.adam_m.as<float>(), s.adam_v.as<float>(), gr, kNParams, (float)(lr / bc1),
+        (float)std::sqrt(bc2), b1, b2, 1e-8f);
     rc = publish(c, s);
     if (rc) return rc;
   }

@@ -795,9 +795,12 @@ __global__ void reduce_parts_kernel(const float *part, int nparts, long long n, 
   grad[i] = v;
 }
 
-// Adam on the FP32 masters; bias-corrected step size lr_t precomputed on the host.
-__global__ void adam_kernel(float *w, float *m, float *v, const float *grad, long long n, float lr_t, float b1,
-                            float b2, float eps) {
+// Adam on the FP32 masters (Kingma & Ba, with the bias corrections applied as torch.optim.Adam
+// applies them): m = b1 m + (1-b1) g, v = b2 v + (1-b2) g^2,
+// w -= (lr / bc1) * m / (sqrt(v) / sqrt(bc2) + eps), with bc1 = 1 - b1^t and bc2 = 1 - b2^t
+// precomputed on the host as step = lr / bc1 and bc2_sqrt = sqrt(bc2).
+__global__ void adam_kernel(float *w, float *m, float *v, const float *grad, long long n, float step, float bc2_sqrt,
+                            float b1, float b2, float eps) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float gr = grad[i];
@@ -805,7 +808,7 @@ __global__ void adam_kernel(float *w, float *m, float *v, const float *grad, lon
   const float vi = b2 * v[i] + (1.f - b2) * gr * gr;
   m[i] = mi;
   v[i] = vi;
-  w[i] -= lr_t * mi / (sqrtf(vi) + eps);
+  w[i] -= step * (mi / (sqrtf(vi) / bc2_sqrt + eps));
 }
 
 // BF16 copies of a [rows][cols] FP32 master: plain (optional) and transposed (optional).

@@ -22,6 +22,19 @@ REF_DIR = os.path.join(HERE, "_ref")
 _libs = {}
 
 
+def reference_root() -> str:
+    """Where the reference tree is: oracle/Makefile's BUDE_REFERENCE setting (the environment
+    variable of that name overrides it).  The tree exists only on the machine that makes fixtures."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-reference"], stdout=subprocess.PIPE,
+                       stderr=subprocess.DEVNULL, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
+def reference_tree_present() -> bool:
+    root = reference_root()
+    return bool(root) and os.path.isfile(os.path.join(root, "src", "main.cpp"))
+
+
 def build(ref: bool = False) -> None:
     """make the restatement (and, with ref=True, the reference itself from REF)."""
     targets = ["all"] + (["ref"] if ref else [])

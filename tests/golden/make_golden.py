@@ -22,7 +22,7 @@ Fixtures:
               FP32, far but finite translations and a huge finite angle planted at fixed poses;
               energies from the reference's SerialBude<1>::fasten (NaN where it gives NaN)
 
-Usage (from the repository root):  python tests/golden/make_golden.py [--reference /root/reference]
+Usage (from the repository root):  python tests/golden/make_golden.py [--reference DIR]  (default: oracle/Makefile's BUDE_REFERENCE)
 """
 from __future__ import annotations
 
@@ -97,7 +97,7 @@ def nonfinite_deck() -> Deck:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=oracle.reference_root())
     ap.add_argument("--only", default="", help="comma-separated fixture names to regenerate (default: all)")
     args = ap.parse_args()
     only = set(filter(None, args.only.split(",")))

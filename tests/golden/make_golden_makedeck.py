@@ -20,7 +20,7 @@ Expected outputs:
                          poses.in and its CPU ref_energies.out
   conformations.f32      the two conformations of conf_ligand.mol2 as x, y, z floats, parsed here
 
-Usage (from the repository root):  python tests/golden/make_golden_makedeck.py [--reference /root/reference]
+Usage (from the repository root):  python tests/golden/make_golden_makedeck.py [--reference DIR]  (default: oracle/Makefile's BUDE_REFERENCE)
 """
 from __future__ import annotations
 
@@ -37,6 +37,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 OUT = os.path.join(HERE, "makedeck")
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
 
 INPUTS = {
     "by_atom.bhff": "bhffs/2_heavy_by-atom_2016-v1.bhff",
@@ -74,7 +77,7 @@ def conformations(mol2_path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=oracle.reference_root())
     args = ap.parse_args()
     raw = os.path.join(args.reference, "makedeck", "raw")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "makedeck", f"REF={args.reference}"], check=True)

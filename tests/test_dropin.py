@@ -9,12 +9,13 @@ import subprocess
 
 import pytest
 
+import oracle
 from conftest import ROOT
 
-REF = "/root/reference"
+REF = oracle.reference_root()
 
 
-@pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "src", "main.cpp")), reason="reference tree not present")
+@pytest.mark.skipif(not oracle.reference_tree_present(), reason="reference tree not present")
 def test_reference_driver_compiles_with_gb300_model(tmp_path):
     from minibude_gb300 import build
     build.build_library()
