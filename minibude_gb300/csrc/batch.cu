@@ -191,6 +191,7 @@ template <int P, int U> static int batch_prepare_pu(int w, size_t smem, int *per
   case 81: CALL(8, 1); break;                                                                                          \
   case 82: CALL(8, 2); break;                                                                                          \
   case 84: CALL(8, 4); break;                                                                                          \
+  case 142: CALL(14, 2); break;                                                                                        \
   case 161: CALL(16, 1); break;                                                                                        \
   case 162: CALL(16, 2); break;                                                                                        \
   default: CALL(16, 4); break;                                                                                         \

@@ -133,14 +133,15 @@ void release_batch(Context &c);
 int enqueue_batch(Context &c, const bude_launch_cfg &cfg, int per_ligand);
 // Cut a ligand's n poses into batch-kernel items of at most ppb = ppwi * wgsize poses: full blocks,
 // then the remainder r.  The batch kernel runs an item of at most ppb/2 or ppb/4 poses with half or
-// a quarter of the poses per thread (a quarter from 8 poses per thread up), so with ppwi >= 8 a
-// remainder ppb/2 < r <= 3ppb/4 is cut into ppb/2 + the rest: 3/4 of a full item's work.
+// a quarter of the poses per thread (a quarter from 8 poses per thread up), so with ppwi 8 or 16 a
+// remainder ppb/2 < r <= 3ppb/4 is cut into ppb/2 + the rest: 3/4 of a full item's work.  (With 14
+// poses per thread, a shape sized for one item per ligand, halves would run 7 poses in 4 pairs.)
 // f(first pose offset within the ligand, pose count) is called per item, in pose order.
 template <class F> inline void for_each_item(long long n, int ppwi, int ppb, F &&f) {
   long long p = 0;
   for (; n - p >= ppb; p += ppb) f(p, ppb);
   const int r = (int)(n - p);
-  if (ppwi >= 8 && 2 * r > ppb && 4 * r <= 3 * ppb) {
+  if ((ppwi == 8 || ppwi == 16) && 2 * r > ppb && 4 * r <= 3 * ppb) {
     f(p, ppb / 2);
     f(p + ppb / 2, r - ppb / 2);
   } else if (r > 0) {

@@ -422,13 +422,17 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
   int with_picks = 0;
   for (int l = 0; l < nl; ++l) with_picks += counts[2 * l] + counts[2 * l + 1] > 0;
   const long long per_lig = with_picks ? ncomp / with_picks : 0;
-  bude_launch_cfg small = overlap         ? bude_launch_cfg{4, 128, cfg.split, cfg.tile, 2, 0}
-                          : per_lig >= 128 ? bude_launch_cfg{8, 32, cfg.split, cfg.tile, 4, 0}
-                                           : bude_launch_cfg{4, 32, cfg.split, cfg.tile, 2, 0};
+  bude_launch_cfg small = overlap                          ? bude_launch_cfg{4, 128, cfg.split, cfg.tile, 2, 0}
+                          : (per_lig > 256 && per_lig <= 448) ? bude_launch_cfg{14, 32, cfg.split, cfg.tile, 2, 0}
+                          : per_lig >= 128                  ? bude_launch_cfg{8, 32, cfg.split, cfg.tile, 4, 0}
+                                                            : bude_launch_cfg{4, 32, cfg.split, cfg.tile, 2, 0};
   if (sc.rescore.ppwi != 0) {
     small = bude_launch_cfg{sc.rescore.ppwi, sc.rescore.wgsize, cfg.split, sc.rescore.tile > 0 ? sc.rescore.tile : cfg.tile,
                             sc.rescore.unroll, 0};
-    rc = check_cfg(c, small);
+    const bool rescore_only = small.ppwi == 14 && small.unroll == 2; // a batch-kernel shape of the rescoring
+    bude_launch_cfg chk = small;
+    if (rescore_only) chk.ppwi = 16;
+    rc = check_cfg(c, chk);
     if (rc) return rc;
     if (cfg.tile % small.tile) return set_error(BUDE_ERR_ARG, "the rescoring tile must divide the exact tile");
   }

@@ -331,7 +331,8 @@ static int ensure_train_scratch(Surrogate &s, long long rows, int batch, int nbl
   if (!rc) rc = s.part_w4.reserve((size_t)nblk * kHid * 4, "w4 parts");
   if (!rc) rc = s.part_b.reserve((size_t)nblk * 4 * kHid * 4, "bias parts");
   if (!rc) rc = s.part_emb.reserve((size_t)nblk * kMaxTypes * kEmb * 4, "embedding parts");
-  if (!rc) rc = s.part_w.reserve((size_t)nchunks * kHid * kHid * 4, "weight parts");
+  // one region per layer (W3, W2: 128 x 128; W1: 128 x 32), all reduced by one launch
+  if (!rc) rc = s.part_w.reserve((size_t)nchunks * kHid * (2 * kHid + kFeat) * 4, "weight parts");
   return rc;
 }
 
@@ -380,14 +381,22 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   b.part_b = s.part_b.as<float>();
   b.part_emb = s.part_emb.as<float>();
   train_backward_kernel<<<nblk, kMlpThreads, sizeof(BwdSmem), c.stream>>>(b);
+  ReduceSegs red{};
   auto reduce = [&](const float *part, int nparts, long long n, long long stride, float *dst) {
-    reduce_parts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c.stream>>>(part, nparts, n, stride, dst);
+    const int k = red.nseg++;
+    red.part[k] = part;
+    red.dst[k] = dst;
+    red.stride[k] = stride;
+    red.n[k] = (int)n;
+    red.nparts[k] = nparts;
+    red.first[k + 1] = red.first[k] + (int)n;
   };
   // layer weight gradients
   struct L { const __nv_bfloat16 *dz, *hin; int kin, act; long long off; };
   const L layers[3] = {{s.dZ3.as<__nv_bfloat16>(), s.Z2.as<__nv_bfloat16>(), kHid, 1, kOffW3},
                        {s.dZ2.as<__nv_bfloat16>(), s.Z1.as<__nv_bfloat16>(), kHid, 1, kOffW2},
                        {s.dZ1.as<__nv_bfloat16>(), s.X.as<__nv_bfloat16>(), kFeat, 0, kOffW1}};
+  float *part_w = s.part_w.as<float>();
   for (const L &l : layers) {
     WgradArgs w;
     w.dZ = l.dz;
@@ -395,10 +404,11 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     w.apply_act = l.act;
     w.rows = (int)rows;
     w.chunk_rows = chunk;
-    w.part = s.part_w.as<float>();
+    w.part = part_w;
     if (l.kin == kHid) wgrad_kernel<kHid><<<nchunks, kMlpThreads, 0, c.stream>>>(w);
     else wgrad_kernel<kFeat><<<nchunks, kMlpThreads, 0, c.stream>>>(w);
-    reduce(s.part_w.as<float>(), nchunks, (long long)kHid * l.kin, (long long)kHid * l.kin, gr + l.off);
+    reduce(part_w, nchunks, (long long)kHid * l.kin, (long long)kHid * l.kin, gr + l.off);
+    part_w += (size_t)nchunks * kHid * l.kin;
   }
   reduce(s.part_w4.as<float>(), nblk, kHid, kHid, gr + kOffW4);
   reduce(s.part_b.as<float>(), nblk, kHid, 4 * kHid, gr + kOffB1);
@@ -406,6 +416,8 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   reduce(s.part_b.as<float>() + 2 * kHid, nblk, kHid, 4 * kHid, gr + kOffB3);
   reduce(s.part_b.as<float>() + 3 * kHid, nblk, 1, 4 * kHid, gr + kOffB4);
   reduce(s.part_emb.as<float>(), nblk, kMaxTypes * kEmb, kMaxTypes * kEmb, gr + kOffEmb);
+  reduce_segments_kernel<<<(unsigned)(((long long)red.first[red.nseg] * kReduceLanes + 255) / 256), 256, 0,
+                           c.stream>>>(red);
   if (lr > 0.f) {
     s.step++;
     const float b1 = 0.9f, b2 = 0.999f;

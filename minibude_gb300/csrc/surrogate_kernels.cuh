@@ -777,22 +777,39 @@ __global__ void __launch_bounds__(kMlpThreads) wgrad_kernel(WgradArgs a) {
   }
 }
 
-// grad[i] = sum over parts of part[p][i], in part order.
-// Eight parts are loaded ahead of their adds, which stay in part order.
-__global__ void reduce_parts_kernel(const float *part, int nparts, long long n, long long stride, float *grad) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+// The per-step gradient reductions in one launch: segment k sums parts [0, nparts) of
+// part[p * stride + i] into dst[i] for i < n.  Eight threads share an element: thread j adds parts
+// j, j + 8, j + 16, ... in order, then the eight sums are combined by a fixed butterfly, so the
+// result is the same bits on every run.
+constexpr int kMaxReduceSegs = 10;
+constexpr int kReduceLanes = 8;
+
+struct ReduceSegs {
+  const float *part[kMaxReduceSegs];
+  float *dst[kMaxReduceSegs];
+  long long stride[kMaxReduceSegs];
+  int n[kMaxReduceSegs];
+  int nparts[kMaxReduceSegs];
+  int first[kMaxReduceSegs + 1]; // prefix sums of n: element e belongs to segment k with first[k] <= e
+  int nseg;
+};
+
+__global__ void __launch_bounds__(256) reduce_segments_kernel(const ReduceSegs r) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = gt / kReduceLanes, j = gt % kReduceLanes;
+  const bool live = e < r.first[r.nseg];
+  int k = 0;
+  while (live && k + 1 < r.nseg && r.first[k + 1] <= e) ++k;
   float v = 0.f;
-  int p = 0;
-  for (; p + 8 <= nparts; p += 8) {
-    float x[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) x[j] = part[(long long)(p + j) * stride + i];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) v += x[j];
+  if (live) {
+    const int i = e - r.first[k];
+    const float *part = r.part[k] + i;
+    const long long stride = r.stride[k];
+    for (int p = j; p < r.nparts[k]; p += kReduceLanes) v += part[(long long)p * stride];
   }
-  for (; p < nparts; ++p) v += part[(long long)p * stride + i];
-  grad[i] = v;
+#pragma unroll
+  for (int o = 1; o < kReduceLanes; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (live && j == 0) r.dst[k][e - r.first[k]] = v;
 }
 
 // Adam on the FP32 masters (Kingma & Ba, with the bias corrections applied as torch.optim.Adam
