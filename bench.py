@@ -614,11 +614,12 @@ def run_screen(args, dist: Dist):
     ex_ms = [ctx.run_batch(cfg) for _ in range(max(2, args.steps // 2))]
     exact = ctx.download_batch()
     exhaustive_ms = float(np.mean(ex_ms))
-    # The screen's exact kernel: the exhaustive shape with the protein cut into 16 slices, so the
-    # rescoring's few hundred poses per ligand still spread over every block slot (measured on this
-    # batch: 26.2 ms of rescoring at 14-16 slices, 26.8 at 7-8, 28.2 at 5).
+    # The screen's exact kernel: the exhaustive shape with the protein cut into 21 slices of 128
+    # records staged 32 at a time, so the rescoring's few hundred poses per ligand still spread over
+    # every block slot (measured on this batch, rescoring with 14 poses per thread: 22.9 ms at 21
+    # slices x 32-record stages, 23.1 at 16 x 32 or 21 x 64, 23.8 at 16 x 64, 25.8 at 8 x 64).
     from minibude_gb300.capi import BudeLaunchCfg
-    scfg = BudeLaunchCfg(cfg.ppwi, cfg.wgsize, 16, cfg.tile, cfg.unroll, 0)
+    scfg = BudeLaunchCfg(cfg.ppwi, cfg.wgsize, 21, 32, cfg.unroll, 0)
     for _ in range(max(args.warmup, 1)):
         ctx.screen(scfg, top_frac=0.02, audit_frac=0.005, audit_tol=0.05, seed=7)
     launches0 = ctx.launch_count()
