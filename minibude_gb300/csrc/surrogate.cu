@@ -20,6 +20,7 @@
 #include "internal.h"
 #include "score_tc.cuh"
 #include "surrogate_kernels.cuh"
+#include "wgrad_tc.cuh"
 
 namespace bude {
 
@@ -48,7 +49,7 @@ struct Surrogate {
   FieldGrid fg{};
   long long step = 0;
   // training scratch
-  DevBuf X, row_type, Z1, Z2, Z3, dZ1, dZ2, dZ3, y, dy, pred, loss, part_w4, part_b, part_emb, part_w;
+  DevBuf X, row_type, Z1, Z2, Z3, dZ1, dZ2, dZ3, y, dy, pred, loss, dsum, part_w, S_sum;
   DevBuf labels, pose_lig_first, pose_lig_n, epoch_pose, epoch_rowoff;
   long long rows_cap = 0;
   // scoring
@@ -79,8 +80,8 @@ void release_surrogate(Context &c) {
   release_textures(s);
   DevBuf *all[] = {&s.params, &s.adam_m, &s.adam_v, &s.grads, &s.emb_bf, &s.w1_bf, &s.w2_bf, &s.w3_bf,
                    &s.w1t_bf, &s.w2t_bf, &s.w3t_bf, &s.grid, &s.protein4, &s.X, &s.row_type, &s.Z1,
-                   &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3, &s.y, &s.dy, &s.pred, &s.loss, &s.part_w4,
-                   &s.part_b, &s.part_emb, &s.part_w, &s.labels, &s.pose_lig_first, &s.pose_lig_n,
+                   &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3, &s.y, &s.dy, &s.pred, &s.loss, &s.dsum,
+                   &s.part_w, &s.S_sum, &s.labels, &s.pose_lig_first, &s.pose_lig_n,
                    &s.epoch_pose, &s.epoch_rowoff, &s.items, &s.scores};
   for (DevBuf *b : all) b->release();
   delete c.surrogate;
@@ -137,6 +138,8 @@ static int set_smem_limits() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(train_backward_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WgTcSmem));
   if (e != cudaSuccess) return cuda_error(e, "surrogate shared-memory limits");
   done = true;
   return BUDE_OK;
@@ -234,6 +237,7 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
   if (rc) return rc;
   cudaError_t e = copy_sync(c, s.params.ptr, p.data(), pb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = fill_sync(c, s.adam_m.ptr, 0, pb);
+  if (e == cudaSuccess) e = fill_sync(c, s.grads.ptr, 0, pb); // the padding after b4 is never written
   if (e == cudaSuccess) e = fill_sync(c, s.adam_v.ptr, 0, pb);
   if (e != cudaSuccess) return cuda_error(e, "surrogate init");
 
@@ -313,7 +317,7 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
   return BUDE_OK;
 }
 
-static int ensure_train_scratch(Surrogate &s, long long rows, int batch, int nblk, int nchunks) {
+static int ensure_train_scratch(Surrogate &s, long long rows, int batch, int wg_blocks) {
   int rc = BUDE_OK;
   if (rows > s.rows_cap) {
     const size_t r = (size_t)rows;
@@ -328,11 +332,9 @@ static int ensure_train_scratch(Surrogate &s, long long rows, int batch, int nbl
   }
   if (!rc) rc = s.pred.reserve((size_t)batch * 4, "pred");
   if (!rc) rc = s.loss.reserve((size_t)batch * 4, "loss");
-  if (!rc) rc = s.part_w4.reserve((size_t)nblk * kHid * 4, "w4 parts");
-  if (!rc) rc = s.part_b.reserve((size_t)nblk * 4 * kHid * 4, "bias parts");
-  if (!rc) rc = s.part_emb.reserve((size_t)nblk * kMaxTypes * kEmb * 4, "embedding parts");
-  // one region per layer (W3, W2: 128 x 128; W1: 128 x 32), all reduced by one launch
-  if (!rc) rc = s.part_w.reserve((size_t)nchunks * kHid * (2 * kHid + kFeat) * 4, "weight parts");
+  if (!rc) rc = s.dsum.reserve((size_t)batch * 4, "per-pose dy sums");
+  if (!rc) rc = s.part_w.reserve((size_t)std::max(wg_blocks, 1) * kWgPart * 4, "gradient parts");
+  if (!rc) rc = s.S_sum.reserve((size_t)kHid * kMaxTypes * 4, "per-type dz1 sums");
   return rc;
 }
 
@@ -350,9 +352,9 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   const MlpWeights W = weights(s);
   const int tiles = (int)((rows + kRowsPerCta - 1) / kRowsPerCta);
   const int nblk = std::min(tiles, 2 * std::max(c.num_sms, 1));
-  const int chunk = 2048;
-  const int nchunks = (int)((rows + chunk - 1) / chunk);
-  int rc = ensure_train_scratch(s, rows, nb, nblk, nchunks);
+  // One gradient block per SM, each with at least one 128-row tile.
+  const int wg_grid = (int)std::min<long long>((rows + kWgTile - 1) / kWgTile, std::max(c.num_sms, 1));
+  int rc = ensure_train_scratch(s, rows, nb, wg_grid);
   if (rc) return rc;
   train_features_kernel<<<(nb * 32 + 255) / 256, 256, 0, c.stream>>>(W, s.fg, c.b_ligands.as<float4>(),
                                                                        c.b_xform.as<float4>(), m,
@@ -362,9 +364,8 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
       s.Z3.as<__nv_bfloat16>(), s.y.as<float>());
   train_loss_kernel<<<(nb + 127) / 128, 128, 0, c.stream>>>(m, s.y.as<float>(), p + kOffB4, s.labels.as<float>(),
                                                           s.pred.as<float>(), s.loss.as<float>(), s.dy.as<float>(),
-                                                          1.f / (float)nb);
+                                                          s.dsum.as<float>(), 1.f / (float)nb);
   BwdArgs b;
-  b.w1t = s.w1t_bf.as<__nv_bfloat16>();
   b.w2t = s.w2t_bf.as<__nv_bfloat16>();
   b.w3t = s.w3t_bf.as<__nv_bfloat16>();
   b.w4 = p + kOffW4;
@@ -372,15 +373,27 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   b.Z2 = s.Z2.as<__nv_bfloat16>();
   b.Z3 = s.Z3.as<__nv_bfloat16>();
   b.dy = s.dy.as<float>();
-  b.row_type = s.row_type.as<int>();
   b.rows = (int)rows;
   b.dZ1 = s.dZ1.as<__nv_bfloat16>();
   b.dZ2 = s.dZ2.as<__nv_bfloat16>();
   b.dZ3 = s.dZ3.as<__nv_bfloat16>();
-  b.part_w4 = s.part_w4.as<float>();
-  b.part_b = s.part_b.as<float>();
-  b.part_emb = s.part_emb.as<float>();
   train_backward_kernel<<<nblk, kMlpThreads, sizeof(BwdSmem), c.stream>>>(b);
+  // Weight, bias and embedding gradients on the tensor cores (wgrad_tc.cuh): per-block partial
+  // sums over contiguous row tiles, folded in block order.
+  WgTcArgs w;
+  w.X = s.X.as<__nv_bfloat16>();
+  w.row_type = s.row_type.as<int>();
+  w.Z1 = s.Z1.as<__nv_bfloat16>();
+  w.Z2 = s.Z2.as<__nv_bfloat16>();
+  w.Z3 = s.Z3.as<__nv_bfloat16>();
+  w.dZ1 = s.dZ1.as<__nv_bfloat16>();
+  w.dZ2 = s.dZ2.as<__nv_bfloat16>();
+  w.dZ3 = s.dZ3.as<__nv_bfloat16>();
+  w.dy = s.dy.as<float>();
+  w.rows = (int)rows;
+  w.part = s.part_w.as<float>();
+  w.err = c.err.as<unsigned int>();
+  wgrad_tc_kernel<<<wg_grid, kWgThreads, sizeof(WgTcSmem), c.stream>>>(w);
   ReduceSegs red{};
   auto reduce = [&](const float *part, int nparts, long long n, long long stride, float *dst) {
     const int k = red.nseg++;
@@ -391,33 +404,20 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     red.nparts[k] = nparts;
     red.first[k + 1] = red.first[k] + (int)n;
   };
-  // layer weight gradients
-  struct L { const __nv_bfloat16 *dz, *hin; int kin, act; long long off; };
-  const L layers[3] = {{s.dZ3.as<__nv_bfloat16>(), s.Z2.as<__nv_bfloat16>(), kHid, 1, kOffW3},
-                       {s.dZ2.as<__nv_bfloat16>(), s.Z1.as<__nv_bfloat16>(), kHid, 1, kOffW2},
-                       {s.dZ1.as<__nv_bfloat16>(), s.X.as<__nv_bfloat16>(), kFeat, 0, kOffW1}};
-  float *part_w = s.part_w.as<float>();
-  for (const L &l : layers) {
-    WgradArgs w;
-    w.dZ = l.dz;
-    w.Hin = l.hin;
-    w.apply_act = l.act;
-    w.rows = (int)rows;
-    w.chunk_rows = chunk;
-    w.part = part_w;
-    if (l.kin == kHid) wgrad_kernel<kHid><<<nchunks, kMlpThreads, 0, c.stream>>>(w);
-    else wgrad_kernel<kFeat><<<nchunks, kMlpThreads, 0, c.stream>>>(w);
-    reduce(part_w, nchunks, (long long)kHid * l.kin, (long long)kHid * l.kin, gr + l.off);
-    part_w += (size_t)nchunks * kHid * l.kin;
-  }
-  reduce(s.part_w4.as<float>(), nblk, kHid, kHid, gr + kOffW4);
-  reduce(s.part_b.as<float>(), nblk, kHid, 4 * kHid, gr + kOffB1);
-  reduce(s.part_b.as<float>() + kHid, nblk, kHid, 4 * kHid, gr + kOffB2);
-  reduce(s.part_b.as<float>() + 2 * kHid, nblk, kHid, 4 * kHid, gr + kOffB3);
-  reduce(s.part_b.as<float>() + 3 * kHid, nblk, 1, 4 * kHid, gr + kOffB4);
-  reduce(s.part_emb.as<float>(), nblk, kMaxTypes * kEmb, kMaxTypes * kEmb, gr + kOffEmb);
+  const float *part = s.part_w.as<float>();
+  reduce(part + kWgOffW3, wg_grid, kHid * kHid, kWgPart, gr + kOffW3);
+  reduce(part + kWgOffB3, wg_grid, kHid, kWgPart, gr + kOffB3);
+  reduce(part + kWgOffW2, wg_grid, kHid * kHid, kWgPart, gr + kOffW2);
+  reduce(part + kWgOffB2, wg_grid, kHid, kWgPart, gr + kOffB2);
+  reduce(part + kWgOffW1, wg_grid, kHid * kFeat, kWgPart, gr + kOffW1);
+  reduce(part + kWgOffB1, wg_grid, kHid, kWgPart, gr + kOffB1);
+  reduce(part + kWgOffW4, wg_grid, kHid, kWgPart, gr + kOffW4);
+  reduce(part + kWgOffS, wg_grid, kHid * kMaxTypes, kWgPart, s.S_sum.as<float>());
+  reduce(s.dsum.as<float>(), nb, 1, 1, gr + kOffB4);
   reduce_segments_kernel<<<(unsigned)(((long long)red.first[red.nseg] * kReduceLanes + 255) / 256), 256, 0,
                            c.stream>>>(red);
+  emb_grad_kernel<<<(kMaxTypes * kEmb + 255) / 256, 256, 0, c.stream>>>(s.S_sum.as<float>(),
+                                                                       s.w1_bf.as<__nv_bfloat16>(), gr + kOffEmb);
   if (lr > 0.f) {
     s.step++;
     const float b1 = 0.9f, b2 = 0.999f;
@@ -637,7 +637,7 @@ int surrogate_features(Context &c, const int *poses, int n, float *X, int *types
   const long long rows = ro[n];
   rc = s.epoch_pose.reserve((size_t)n * 4, "poses");
   if (!rc) rc = s.epoch_rowoff.reserve((size_t)(n + 1) * 4, "row offsets");
-  if (!rc) rc = ensure_train_scratch(s, std::max(rows, 1LL), n, 1, 1);
+  if (!rc) rc = ensure_train_scratch(s, std::max(rows, 1LL), n, 1);
   if (rc) return rc;
   cudaError_t e = copy_sync(c, s.epoch_pose.ptr, poses, (size_t)n * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = copy_sync(c, s.epoch_rowoff.ptr, ro.data(), ro.size() * 4, cudaMemcpyHostToDevice);

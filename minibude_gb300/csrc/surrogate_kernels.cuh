@@ -439,11 +439,11 @@ __global__ void __launch_bounds__(kMlpThreads) train_forward_kernel(MlpWeights W
 
 // Per batch pose: prediction = sum of its rows' y + natlig * b4; loss on the compressed scale
 // c(E) = S * asinh(E / S); dy (per row) = dLoss/dprediction.  loss_out[i] = the pose's squared
-// error (summed on the host, deterministic).
+// error (summed on the host, deterministic); dsum[i] = the sum of dy over the pose's rows.
 constexpr float kLossScale = 20.f;
 
 __global__ void train_loss_kernel(RowMap m, const float *y, const float *b4, const float *labels, float *pred,
-                                  float *loss_out, float *dy, float inv_batch) {
+                                  float *loss_out, float *dy, float *dsum, float inv_batch) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.nposes) return;
   const int p = m.pose[i];
@@ -457,35 +457,26 @@ __global__ void train_loss_kernel(RowMap m, const float *y, const float *b4, con
   loss_out[i] = d * d;
   const float grad = 2.f * d * rsqrtf(1.f + (s / kLossScale) * (s / kLossScale)) * inv_batch;
   for (int a = 0; a < n; ++a) dy[row0 + a] = grad;
+  dsum[i] = (float)n * grad; // the pose's share of the b4 gradient (sum of dy over its rows)
 }
 
-// Backward through the layers for a tile of rows: writes dz3, dz2, dz1 (BF16) for the weight
-// gradients, and per block: d w4 / d b4 partials, bias partials and embedding partials (each
-// summed in a fixed order, so the whole backward pass is deterministic).
+// Backward through the layers for a tile of rows: dz3 = dy * w4 * act'(z3), then
+// dz2 = (dz3 W3) * act'(z2) and dz1 = (dz2 W2) * act'(z1) on mma.sync, each stored as BF16 for the
+// gradient kernel (wgrad_tc.cuh), which also forms the bias, output-weight and embedding gradients.
 struct BwdArgs {
-  const __nv_bfloat16 *w1t; // [32][128]  (W1 transposed: in x out)
-  const __nv_bfloat16 *w2t; // [128][128]
+  const __nv_bfloat16 *w2t; // [128][128]  (W2 transposed: in x out)
   const __nv_bfloat16 *w3t; // [128][128]
   const float *w4;
   const __nv_bfloat16 *Z1, *Z2, *Z3;
   const float *dy;
-  const int *row_type;
   int rows;
   __nv_bfloat16 *dZ1, *dZ2, *dZ3;
-  float *part_w4;  // [blocks][128]
-  float *part_b;   // [blocks][4][128]  (b1, b2, b3, b4 in slot 3 col 0)
-  float *part_emb; // [blocks][kMaxTypes][16]
 };
 
 struct BwdSmem {
   __nv_bfloat16 w2t[kHid * kLdH];
   __nv_bfloat16 w3t[kHid * kLdH];
-  __nv_bfloat16 w1t[kFeat * kLdH];
   float w4[kHid];
-  float red[8][kHid];        // per-warp column sums
-  float demb[kRowsPerCta][kEmb];
-  int type[kRowsPerCta];
-  float emb_acc[kMaxTypes][kEmb];
 };
 
 __global__ void __launch_bounds__(kMlpThreads, 2) train_backward_kernel(BwdArgs a) {
@@ -496,44 +487,9 @@ __global__ void __launch_bounds__(kMlpThreads, 2) train_backward_kernel(BwdArgs 
     *reinterpret_cast<uint4 *>(&s.w2t[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(a.w2t) + i);
     *reinterpret_cast<uint4 *>(&s.w3t[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(a.w3t) + i);
   }
-  for (int i = threadIdx.x; i < kFeat * kHid / 8; i += blockDim.x) {
-    const int o = i / (kHid / 8), k8 = i % (kHid / 8);
-    *reinterpret_cast<uint4 *>(&s.w1t[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(a.w1t) + i);
-  }
   for (int i = threadIdx.x; i < kHid; i += blockDim.x) s.w4[i] = a.w4[i];
-  for (int i = threadIdx.x; i < kMaxTypes * kEmb; i += blockDim.x) (&s.emb_acc[0][0])[i] = 0.f;
   __syncthreads(); // the staged weights are read by every warp below
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  // Block-level partials accumulate in registers of threads < 128 (one column each).
-  float acc_b[4] = {0.f, 0.f, 0.f, 0.f};
-  float acc_w4 = 0.f;
-
-  // Column sums of a warp's 16 x 128 BF16-pair values (v[j][0] row g, v[j][1] row g+8) into
-  // s.red[warp][col]; values are first summed over the 8 row groups with shuffles in a fixed order.
-  auto colsum = [&](const float (&v)[16][4]) {
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      float c0 = v[j][0] + v[j][2], c1 = v[j][1] + v[j][3];
-#pragma unroll
-      for (int off = 4; off < 32; off <<= 1) {
-        c0 += __shfl_xor_sync(0xffffffffu, c0, off);
-        c1 += __shfl_xor_sync(0xffffffffu, c1, off);
-      }
-      if (g == 0) {
-        s.red[warp][j * 8 + 2 * t] = c0;
-        s.red[warp][j * 8 + 2 * t + 1] = c1;
-      }
-    }
-  };
-  auto fold = [&](float &dst) { // sum the 8 warps' column sums in order (threads < 128)
-    __syncthreads();
-    if (threadIdx.x < kHid) {
-      float v = 0.f;
-      for (int w = 0; w < 8; ++w) v += s.red[w][threadIdx.x];
-      dst += v;
-    }
-    __syncthreads();
-  };
 
   for (int tile = blockIdx.x; tile * kRowsPerCta < a.rows; tile += gridDim.x) {
     const int base = tile * kRowsPerCta;
@@ -551,8 +507,8 @@ __global__ void __launch_bounds__(kMlpThreads, 2) train_backward_kernel(BwdArgs 
       if (v0) *reinterpret_cast<uint32_t *>(dZ + (long long)r0 * kHid + j * 8 + 2 * t) = pack_bf16(d[0], d[1]);
       if (v1) *reinterpret_cast<uint32_t *>(dZ + (long long)r1 * kHid + j * 8 + 2 * t) = pack_bf16(d[2], d[3]);
     };
-    // Layer 4 -> dz3 (and the w4 gradient dy * h3).
-    float dz[16][4], cs[16][4];
+    // Layer 4 -> dz3.
+    float dz[16][4];
     uint32_t A[8][4];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
@@ -563,31 +519,9 @@ __global__ void __launch_bounds__(kMlpThreads, 2) train_backward_kernel(BwdArgs 
       dz[j][1] = dy0 * s.w4[c0 + 1] * act_grad(z[1]);
       dz[j][2] = dy1 * s.w4[c0] * act_grad(z[2]);
       dz[j][3] = dy1 * s.w4[c0 + 1] * act_grad(z[3]);
-      const float2 h0 = unpack_bf16(act_pair(z[0], z[1])), h1 = unpack_bf16(act_pair(z[2], z[3]));
-      cs[j][0] = dy0 * h0.x;
-      cs[j][1] = dy0 * h0.y;
-      cs[j][2] = dy1 * h1.x;
-      cs[j][3] = dy1 * h1.y;
     }
-    colsum(cs);
-    fold(acc_w4);
-    // b4 gradient: sum of dy over the tile's rows (slot 3, column 0), in a fixed order.
-    {
-      float d = (t == 0) ? dy0 + dy1 : 0.f;
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
-      if (lane == 0) s.red[warp][0] = d;
-      for (int j = 1; j < 16 && lane == 0; ++j) s.red[warp][j] = 0.f;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        float v = 0.f;
-        for (int w = 0; w < 8; ++w) v += s.red[w][0];
-        acc_b[3] += v;
-      }
-      __syncthreads();
-    }
-    // dz3 -> BF16 A fragments, store, bias-3 partial.
-    auto to_frags = [&](const float (&d)[16][4], __nv_bfloat16 *dZ, float &bacc) {
+    // dz -> BF16 A fragments of the next product, and stored.
+    auto to_frags = [&](const float (&d)[16][4], __nv_bfloat16 *dZ) {
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         dz_store(dZ, j, d[j]);
@@ -600,10 +534,8 @@ __global__ void __launch_bounds__(kMlpThreads, 2) train_backward_kernel(BwdArgs 
           A[j >> 1][3] = hi;
         }
       }
-      colsum(d);
-      fold(bacc);
     };
-    to_frags(dz, a.dZ3, acc_b[2]);
+    to_frags(dz, a.dZ3);
     // dh2 = dz3 W3 ; dz2 = dh2 * act'(z2)
     float acc[16][4];
     layer_mma<8, kLdH>(acc, A, s.w3t);
@@ -614,7 +546,7 @@ __global__ void __launch_bounds__(kMlpThreads, 2) train_backward_kernel(BwdArgs 
 #pragma unroll
       for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * act_grad(z[q]);
     }
-    to_frags(dz, a.dZ2, acc_b[1]);
+    to_frags(dz, a.dZ2);
     // dh1 = dz2 W2 ; dz1 = dh1 * act'(z1)
     layer_mma<8, kLdH>(acc, A, s.w2t);
 #pragma unroll
@@ -624,156 +556,8 @@ __global__ void __launch_bounds__(kMlpThreads, 2) train_backward_kernel(BwdArgs 
 #pragma unroll
       for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * act_grad(z[q]);
     }
-    to_frags(dz, a.dZ1, acc_b[0]);
-    // dx (embedding columns 0..15) = dz1 W1: two n-tiles of W1^T rows 0..15.
-    {
-      float dx[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
-      for (int kk = 0; kk < 8; ++kk) {
-        uint32_t b[4];
-        const int row = (lane & 7) + ((lane >> 4) << 3);
-        const int col = kk * 16 + ((lane >> 3) & 1) * 8;
-        ldsm_x4(b, s.w1t + row * kLdH + col);
-        mma_bf16(dx[0], A[kk], b[0], b[1]);
-        mma_bf16(dx[1], A[kk], b[2], b[3]);
-      }
-      const int lr0 = warp * 16 + g, lr1 = lr0 + 8;
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        s.demb[lr0][j * 8 + 2 * t] = v0 ? dx[j][0] : 0.f;
-        s.demb[lr0][j * 8 + 2 * t + 1] = v0 ? dx[j][1] : 0.f;
-        s.demb[lr1][j * 8 + 2 * t] = v1 ? dx[j][2] : 0.f;
-        s.demb[lr1][j * 8 + 2 * t + 1] = v1 ? dx[j][3] : 0.f;
-      }
-      if (t == 0) {
-        s.type[lr0] = v0 ? a.row_type[r0] : 0;
-        s.type[lr1] = v1 ? a.row_type[r1] : 0;
-      }
-      __syncthreads();
-      if (threadIdx.x < kEmb) { // thread j owns embedding column j: rows in order
-        for (int r = 0; r < kRowsPerCta; ++r) s.emb_acc[s.type[r]][threadIdx.x] += s.demb[r][threadIdx.x];
-      }
-      __syncthreads();
-    }
-  }
-  if (threadIdx.x < kHid) {
-    a.part_w4[(long long)blockIdx.x * kHid + threadIdx.x] = acc_w4;
-    for (int l = 0; l < 4; ++l) a.part_b[((long long)blockIdx.x * 4 + l) * kHid + threadIdx.x] = acc_b[l];
-  }
-  for (int i = threadIdx.x; i < kMaxTypes * kEmb; i += blockDim.x)
-    a.part_emb[(long long)blockIdx.x * kMaxTypes * kEmb + i] = (&s.emb_acc[0][0])[i];
-}
-
-// Weight gradient partials of one layer: part[chunk] = dZ^T H over `chunk_rows` rows, with
-// H = act(Zin) (or the features X for layer 1, kin = 32).  8 warps x 16 output rows.
-struct WgradArgs {
-  const __nv_bfloat16 *dZ;  // [rows][128]
-  const __nv_bfloat16 *Hin; // [rows][KIN]: pre-activations (apply act) or features
-  int apply_act;
-  int rows;
-  int chunk_rows; // multiple of 16
-  float *part;    // [chunks][128][kin]
-};
-
-// Rows per shared-memory stage of wgrad_kernel: four 16-row k-steps, so one pair of barriers
-// serves four MMA steps and the next stage's loads are in flight while this one computes.
-constexpr int kWgRows = 64;
-
-struct WgradSmem {
-  __nv_bfloat16 dz[kWgRows * kLdH];
-  __nv_bfloat16 h[kWgRows * kLdH];
-};
-
-template <int KIN>
-__global__ void __launch_bounds__(kMlpThreads) wgrad_kernel(WgradArgs a) {
-  __shared__ __align__(16) WgradSmem s;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  constexpr int nt = KIN / 8; // n-tiles of the output row
-  constexpr int kDzVec = kWgRows * kHid / 8;   // 16-byte vectors of dZ per stage
-  constexpr int kHVec = kWgRows * KIN / 8;     // and of H
-  constexpr int kDzPer = kDzVec / kMlpThreads; // per thread
-  constexpr int kHPer = (kHVec + kMlpThreads - 1) / kMlpThreads;
-  static_assert(kDzVec % kMlpThreads == 0, "dZ stage must split evenly over the block");
-  float acc[16][4];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-  const int r_begin = blockIdx.x * a.chunk_rows;
-  const int r_end = min(a.rows, r_begin + a.chunk_rows);
-  // Registers holding the next stage: rows past r_end are zero (as the staging always did).
-  uint4 pd[kDzPer], ph[kHPer];
-  auto fetch = [&](int r) {
-#pragma unroll
-    for (int q = 0; q < kDzPer; ++q) {
-      const int i = threadIdx.x + q * kMlpThreads;
-      const int rr = i / (kHid / 8), k8 = i % (kHid / 8);
-      pd[q] = make_uint4(0, 0, 0, 0);
-      if (r + rr < r_end) pd[q] = *reinterpret_cast<const uint4 *>(a.dZ + (long long)(r + rr) * kHid + k8 * 8);
-    }
-#pragma unroll
-    for (int q = 0; q < kHPer; ++q) {
-      const int i = threadIdx.x + q * kMlpThreads;
-      const int rr = i / (KIN / 8), k8 = i % (KIN / 8);
-      ph[q] = make_uint4(0, 0, 0, 0);
-      if (i < kHVec && r + rr < r_end) {
-        uint4 v = *reinterpret_cast<const uint4 *>(a.Hin + (long long)(r + rr) * KIN + k8 * 8);
-        if (a.apply_act) {
-          uint32_t *w = reinterpret_cast<uint32_t *>(&v);
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const float2 f = unpack_bf16(w[e]);
-            w[e] = act_pair(f.x, f.y);
-          }
-        }
-        ph[q] = v;
-      }
-    }
-  };
-  if (r_begin < r_end) fetch(r_begin);
-  for (int r = r_begin; r < r_end; r += kWgRows) {
-    __syncthreads(); // the previous stage has been read
-#pragma unroll
-    for (int q = 0; q < kDzPer; ++q) {
-      const int i = threadIdx.x + q * kMlpThreads;
-      *reinterpret_cast<uint4 *>(&s.dz[(i / (kHid / 8)) * kLdH + (i % (kHid / 8)) * 8]) = pd[q];
-    }
-#pragma unroll
-    for (int q = 0; q < kHPer; ++q) {
-      const int i = threadIdx.x + q * kMlpThreads;
-      if (i < kHVec) *reinterpret_cast<uint4 *>(&s.h[(i / (KIN / 8)) * kLdH + (i % (KIN / 8)) * 8]) = ph[q];
-    }
-    __syncthreads();
-    if (r + kWgRows < r_end) fetch(r + kWgRows);
-    // 16-row k-steps in row order, none past r_end: the same MMA sequence as one stage per step.
-    for (int ks = 0; ks < kWgRows / 16 && r + ks * 16 < r_end; ++ks) {
-      const __nv_bfloat16 *dz = s.dz + ks * 16 * kLdH, *h = s.h + ks * 16 * kLdH;
-      // A (m = out row, k = data row) = dZ^T: transposed 8x8 loads of dz[r][o].
-      uint32_t af[4];
-      {
-        const int q = lane >> 3;
-        const int row = (lane & 7) + ((q >> 1) << 3);
-        const int col = warp * 16 + ((q & 1) << 3);
-        ldsm_x4_trans(af, dz + row * kLdH + col);
-      }
-#pragma unroll
-      for (int jp = 0; jp < nt / 2; ++jp) {
-        uint32_t b[4];
-        const int q = lane >> 3;
-        const int row = (lane & 7) + ((q & 1) << 3);
-        const int col = jp * 16 + ((q >> 1) << 3);
-        ldsm_x4_trans(b, h + row * kLdH + col);
-        mma_bf16(acc[2 * jp], af, b[0], b[1]);
-        mma_bf16(acc[2 * jp + 1], af, b[2], b[3]);
-      }
-    }
-  }
-  float *out = a.part + (long long)blockIdx.x * kHid * KIN;
-  const int o0 = warp * 16 + g, o1 = o0 + 8;
-#pragma unroll
-  for (int j = 0; j < nt; ++j) {
-    out[o0 * KIN + j * 8 + 2 * t] = acc[j][0];
-    out[o0 * KIN + j * 8 + 2 * t + 1] = acc[j][1];
-    out[o1 * KIN + j * 8 + 2 * t] = acc[j][2];
-    out[o1 * KIN + j * 8 + 2 * t + 1] = acc[j][3];
+    for (int j = 0; j < 16; ++j) dz_store(a.dZ1, j, dz[j]);
   }
 }
 
