@@ -46,6 +46,7 @@ template <int G> struct TcSmem {
   alignas(16) float w4f[kHid];                               // output weights, FP32
   uint4 emb[kMaxTypes * 2];                                  // type embeddings (16 BF16 each)
   alignas(8) uint64_t bar[G];
+  int item[G]; // per group: the tile it took from a work counter (training forward pass)
   uint32_t tmem;
 };
 
@@ -240,6 +241,143 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
       break;
     }
     if (lt < it.w) a.scores[it.z + lt] = e + (float)it.y * b4;
+  }
+  if (failed) {
+    atomicOr(A.err, 1u);
+    if (lt == 0) (void)mbar_wait_bounded(bar, phase ^ 1u); // an outstanding UMMA completes before TMEM goes
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (tid < 32) tmem_dealloc<tc_alloc_cols<G>()>(s.tmem);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Training forward pass on the same machinery: 128-row tiles of the step's (pose, ligand atom)
+// feature rows X instead of poses.  Per tile a group runs layers 1..3 as above and, after each,
+// stores the row's pre-activations z_l as BF16 ([rows][128], the backward pass and the gradient
+// kernel read them) before the activation goes back into `act`; the output layer gives y per row
+// (w4 . h3, without b4: the loss kernel adds natlig * b4 per pose).  Tiles come from a work
+// counter; a row's arithmetic does not depend on which group runs it.
+struct TrainFwdTcArgs {
+  MlpWeights W;
+  const __nv_bfloat16 *X; // [rows][32]
+  int rows;
+  __nv_bfloat16 *Z1, *Z2, *Z3;
+  float *y;
+  unsigned int *err;
+  unsigned int *next; // work counter, zero at launch
+};
+
+__global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_tc_kernel(const TrainFwdTcArgs A) {
+  constexpr int G = kTcGroups;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  TcSmem<G> &s = *reinterpret_cast<TcSmem<G> *>(smem_raw);
+  const int tid = threadIdx.x, g = tid / kTcGroupThreads, lt = tid % kTcGroupThreads;
+  const uint32_t bar_id = 1 + g;
+
+  tc_setup(s, A.W);
+  if (tid == 0) {
+    for (int q = 0; q < G; ++q) mbar_init(&s.bar[q], 1);
+    mbar_fence_init();
+  }
+  if (tid < 32) tmem_alloc<tc_alloc_cols<G>()>(&s.tmem);
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+
+  const uint32_t tmem = s.tmem + (uint32_t)(g * kTcCols);
+  const uint32_t lane_addr = tmem + ((uint32_t)((lt / 32) * 32) << 16);
+  unsigned char *act = s.act[g];
+  const uint32_t act_a = smem_u32(act), ones_a = smem_u32(s.ones);
+  const uint32_t idesc = umma_idesc_bf16(kHid, kHid);
+  uint64_t *bar = &s.bar[g];
+  uint32_t phase = 0;
+  bool failed = false;
+  const int tiles = (A.rows + kTcGroupThreads - 1) / kTcGroupThreads;
+
+  auto hidden = [&](uint32_t w, uint32_t bias, int kdim) {
+    if (lt == 0) {
+      tc_fence_after();
+      const uint32_t sbo = (uint32_t)(kdim / 8) * 128u, bsbo = (kTcBiasK / 8) * 128u;
+      umma_bf16(tmem, umma_desc(ones_a, 128u, bsbo), umma_desc(bias, 128u, bsbo), idesc, 0u);
+      for (int kk = 0; kk < kdim / 16; ++kk)
+        umma_bf16(tmem, umma_desc(act_a + kk * 256u, 128u, sbo), umma_desc(w + kk * 256u, 128u, sbo), idesc, 1u);
+      umma_commit(bar);
+    }
+    if (!mbar_wait_bounded(bar, phase)) failed = true;
+    phase ^= 1u;
+    tc_fence_after();
+  };
+  // z (the accumulators) -> BF16 row of Z in global memory; act(z) -> the next layer's `act` tile,
+  // or, after layer 3, w4 . act(z) -> y.
+  auto epilogue = [&](__nv_bfloat16 *Z, long long row, bool valid, bool to_act, float *yout) {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int c = 0; c < kHid / 32; ++c) {
+      uint32_t v[32];
+      tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
+      tmem_wait_ld();
+      uint32_t zb[16], hb[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const float z0 = __uint_as_float(v[2 * i]), z1 = __uint_as_float(v[2 * i + 1]);
+        zb[i] = pack_bf16(z0, z1);
+        hb[i] = act_pair(z0, z1);
+      }
+      if (valid) {
+        uint4 *dst = reinterpret_cast<uint4 *>(Z + row * kHid + c * 32);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dst[q] = make_uint4(zb[4 * q], zb[4 * q + 1], zb[4 * q + 2], zb[4 * q + 3]);
+      }
+      if (to_act) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c * 32 + q * 8, kHid)) =
+              make_uint4(hb[4 * q], hb[4 * q + 1], hb[4 * q + 2], hb[4 * q + 3]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 16; i += 2) {
+          const float4 w = *reinterpret_cast<const float4 *>(&s.w4f[c * 32 + 2 * i]);
+          acc = fma2(unpack_bf16(hb[i]), make_float2(w.x, w.y), acc);
+          acc = fma2(unpack_bf16(hb[i + 1]), make_float2(w.z, w.w), acc);
+        }
+      }
+    }
+    if (yout && valid) *yout = acc.x + acc.y;
+    if (to_act) fence_proxy_async();
+    tc_fence_before();
+    named_sync(bar_id, kTcGroupThreads);
+  };
+
+  for (;;) {
+    if (lt == 0) s.item[g] = (int)atomicAdd(A.next, 1u);
+    named_sync(bar_id, kTcGroupThreads);
+    const int tile = s.item[g]; // rewritten only after the group's end-of-tile barrier below
+    if (tile >= tiles) break;
+    const long long row = (long long)tile * kTcGroupThreads + lt;
+    const bool valid = row < A.rows;
+    const uint4 *x = reinterpret_cast<const uint4 *>(A.X + row * kFeat);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, q * 8, kFeat)) = valid ? __ldg(x + q) : make_uint4(0, 0, 0, 0);
+    fence_proxy_async();
+    tc_fence_before();
+    if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
+      failed = true;
+      break;
+    }
+    hidden(smem_u32(s.w1), smem_u32(s.bias[0]), kFeat);
+    epilogue(A.Z1, row, valid, true, nullptr);
+    hidden(smem_u32(s.w2), smem_u32(s.bias[1]), kHid);
+    epilogue(A.Z2, row, valid, true, nullptr);
+    hidden(smem_u32(s.w3), smem_u32(s.bias[2]), kHid);
+    epilogue(A.Z3, row, valid, false, A.y + row);
+    if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
+      failed = true;
+      break;
+    }
   }
   if (failed) {
     atomicOr(A.err, 1u);

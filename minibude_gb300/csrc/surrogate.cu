@@ -53,7 +53,7 @@ struct Surrogate {
   DevBuf labels, pose_lig_first, pose_lig_n, epoch_pose, epoch_rowoff;
   long long rows_cap = 0;
   // scoring
-  DevBuf items, scores;
+  DevBuf items, scores, next;
   std::vector<int> item_lig_off; // nligands + 1: first scoring item of each ligand
   long long items_for = -1; // Context::batch_gen the items were built for
   int n_items = 0;
@@ -82,7 +82,7 @@ void release_surrogate(Context &c) {
                    &s.w1t_bf, &s.w2t_bf, &s.w3t_bf, &s.grid, &s.protein4, &s.X, &s.row_type, &s.Z1,
                    &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3, &s.y, &s.dy, &s.pred, &s.loss, &s.dsum,
                    &s.part_w, &s.S_sum, &s.labels, &s.pose_lig_first, &s.pose_lig_n,
-                   &s.epoch_pose, &s.epoch_rowoff, &s.items, &s.scores};
+                   &s.epoch_pose, &s.epoch_rowoff, &s.items, &s.scores, &s.next};
   for (DevBuf *b : all) b->release();
   delete c.surrogate;
   c.surrogate = nullptr;
@@ -140,6 +140,9 @@ static int set_smem_limits() {
                              (int)cudaSharedmemCarveoutMaxShared);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WgTcSmem));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(train_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(TcSmem<kTcGroups>));
   if (e != cudaSuccess) return cuda_error(e, "surrogate shared-memory limits");
   done = true;
   return BUDE_OK;
@@ -359,9 +362,25 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   train_features_kernel<<<(nb * 32 + 255) / 256, 256, 0, c.stream>>>(W, s.fg, c.b_ligands.as<float4>(),
                                                                        c.b_xform.as<float4>(), m,
                                                                        s.X.as<__nv_bfloat16>(), s.row_type.as<int>());
-  train_forward_kernel<<<nblk, kMlpThreads, sizeof(MlpSmem), c.stream>>>(
-      W, s.X.as<__nv_bfloat16>(), (int)rows, s.Z1.as<__nv_bfloat16>(), s.Z2.as<__nv_bfloat16>(),
-      s.Z3.as<__nv_bfloat16>(), s.y.as<float>());
+  {
+    // Forward on the tensor cores (score_tc.cuh): z1, z2, z3 as BF16 and y per row.
+    rc = s.next.reserve(256, "work counter");
+    if (rc) return rc;
+    cudaMemsetAsync(s.next.ptr, 0, sizeof(unsigned int), c.stream);
+    TrainFwdTcArgs f;
+    f.W = W;
+    f.X = s.X.as<__nv_bfloat16>();
+    f.rows = (int)rows;
+    f.Z1 = s.Z1.as<__nv_bfloat16>();
+    f.Z2 = s.Z2.as<__nv_bfloat16>();
+    f.Z3 = s.Z3.as<__nv_bfloat16>();
+    f.y = s.y.as<float>();
+    f.err = c.err.as<unsigned int>();
+    f.next = s.next.as<unsigned int>();
+    const int ftiles = (int)((rows + kTcGroupThreads - 1) / kTcGroupThreads);
+    const int grid = std::max(1, std::min((ftiles + kTcGroups - 1) / kTcGroups, std::max(c.num_sms, 1)));
+    train_forward_tc_kernel<<<grid, kTcGroups * kTcGroupThreads, sizeof(TcSmem<kTcGroups>), c.stream>>>(f);
+  }
   train_loss_kernel<<<(nb + 127) / 128, 128, 0, c.stream>>>(m, s.y.as<float>(), p + kOffB4, s.labels.as<float>(),
                                                           s.pred.as<float>(), s.loss.as<float>(), s.dy.as<float>(),
                                                           s.dsum.as<float>(), 1.f / (float)nb);
