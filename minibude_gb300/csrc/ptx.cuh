@@ -102,6 +102,31 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
   return false;
 }
 
+// The same bounded wait with a suspend-time hint: a waiting thread may sleep in the barrier until
+// the phase completes (or 1 ms passes) instead of probing it again and again, which leaves the
+// shared-memory pipe to the threads doing work.  Used where 128 threads wait on one tensor-core
+// commit at a time.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(1000000u)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait_sleep_bounded(uint64_t *bar, uint32_t parity) {
+  if (mbar_try_wait_sleep(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t it = 1; it < kWaitMaxProbes; ++it) {
+    if (mbar_try_wait_sleep(bar, parity)) return true;
+    if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+  }
+  return false;
+}
+
 // 16-byte read-only global load that the compiler may not hoist out of a loop.
 __device__ __forceinline__ float4 ldg_stream(const float4 *p) {
   float4 v;

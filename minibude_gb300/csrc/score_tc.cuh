@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
     }
   };
   auto layer_wait = [&]() {
-    if (!mbar_wait_bounded(bar, phase)) failed = true;
+    if (!mbar_wait_sleep_bounded(bar, phase)) failed = true;
     phase ^= 1u;
     tc_fence_after();
   };
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
         umma_bf16(tmem, umma_desc(act_a + kk * 256u, 128u, sbo), umma_desc(w + kk * 256u, 128u, sbo), idesc, 1u);
       umma_commit(bar);
     }
-    if (!mbar_wait_bounded(bar, phase)) failed = true;
+    if (!mbar_wait_sleep_bounded(bar, phase)) failed = true;
     phase ^= 1u;
     tc_fence_after();
   };
@@ -374,6 +374,166 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
     epilogue(A.Z2, row, valid, true, nullptr);
     hidden(smem_u32(s.w3), smem_u32(s.bias[2]), kHid);
     epilogue(A.Z3, row, valid, false, A.y + row);
+    if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
+      failed = true;
+      break;
+    }
+  }
+  if (failed) {
+    atomicOr(A.err, 1u);
+    if (lt == 0) (void)mbar_wait_bounded(bar, phase ^ 1u); // an outstanding UMMA completes before TMEM goes
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (tid < 32) tmem_dealloc<tc_alloc_cols<G>()>(s.tmem);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Training backward pass through the hidden layers on the same machinery, per 128-row tile:
+//   dz3 = dy * w4 * act'(z3)                       (FMA pipe, from the stored z3 and dy)
+//   dz2 = (dz3 W3) * act'(z2),  dz1 = (dz2 W2) * act'(z1)   (UMMAs against the transposed weight
+//                                                   copies W3^T, W2^T, FP32 accumulators in TMEM)
+// Each dz is rounded to BF16, stored ([rows][128], the gradient kernel of wgrad_tc.cuh reads them)
+// and written into `act` as the next UMMA's A operand.
+template <int G> struct TcBwdSmem {
+  alignas(128) unsigned char w3t[kHid * kHid * 2]; // W3^T: [in 128][out 128], K-major (K = out)
+  alignas(128) unsigned char w2t[kHid * kHid * 2]; // W2^T
+  alignas(128) unsigned char act[G][kHid * kHid * 2];
+  alignas(16) float w4f[kHid];
+  alignas(8) uint64_t bar[G];
+  int item[G];
+  uint32_t tmem;
+};
+static_assert(sizeof(TcBwdSmem<4>) <= 227 * 1024, "one block per SM fits the 227 KB shared-memory limit");
+
+struct TrainBwdTcArgs {
+  const __nv_bfloat16 *w3t, *w2t; // [in][out] BF16 (the published transposed copies)
+  const float *w4;
+  const __nv_bfloat16 *Z1, *Z2, *Z3;
+  const float *dy;
+  int rows;
+  __nv_bfloat16 *dZ1, *dZ2, *dZ3;
+  unsigned int *err;
+  unsigned int *next; // work counter, zero at launch
+};
+
+__global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward_tc_kernel(const TrainBwdTcArgs A) {
+  constexpr int G = kTcGroups;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  TcBwdSmem<G> &s = *reinterpret_cast<TcBwdSmem<G> *>(smem_raw);
+  const int tid = threadIdx.x, g = tid / kTcGroupThreads, lt = tid % kTcGroupThreads;
+  const uint32_t bar_id = 1 + g;
+
+  to_kmajor(s.w3t, A.w3t, kHid, kHid);
+  to_kmajor(s.w2t, A.w2t, kHid, kHid);
+  for (int i = tid; i < kHid; i += blockDim.x) s.w4f[i] = __ldg(&A.w4[i]);
+  if (tid == 0) {
+    for (int q = 0; q < G; ++q) mbar_init(&s.bar[q], 1);
+    mbar_fence_init();
+  }
+  if (tid < 32) tmem_alloc<tc_alloc_cols<G>()>(&s.tmem);
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+
+  const uint32_t tmem = s.tmem + (uint32_t)(g * kTcCols);
+  const uint32_t lane_addr = tmem + ((uint32_t)((lt / 32) * 32) << 16);
+  unsigned char *act = s.act[g];
+  const uint32_t act_a = smem_u32(act);
+  const uint32_t idesc = umma_idesc_bf16(kHid, kHid);
+  uint64_t *bar = &s.bar[g];
+  uint32_t phase = 0;
+  bool failed = false;
+  const int tiles = (A.rows + kTcGroupThreads - 1) / kTcGroupThreads;
+
+  // D = act * Wt^T over K = 128 (no bias), issued by the group's first thread, then waited for.
+  auto product = [&](uint32_t wt) {
+    fence_proxy_async();
+    tc_fence_before();
+    named_sync(bar_id, kTcGroupThreads);
+    if (lt == 0) {
+      tc_fence_after();
+      constexpr uint32_t sbo = (kHid / 8) * 128u;
+      for (int kk = 0; kk < kHid / 16; ++kk)
+        umma_bf16(tmem, umma_desc(act_a + kk * 256u, 128u, sbo), umma_desc(wt + kk * 256u, 128u, sbo), idesc,
+                  kk ? 1u : 0u);
+      umma_commit(bar);
+    }
+    if (!mbar_wait_sleep_bounded(bar, phase)) failed = true;
+    phase ^= 1u;
+    tc_fence_after();
+  };
+  // 16 dz values (BF16 pairs) of columns [c0, c0 + 32) -> the row of dZ in global memory and,
+  // when to_act, the `act` tile.
+  auto put = [&](__nv_bfloat16 *dZ, long long row, bool valid, int c0, const uint32_t (&d)[16], bool to_act) {
+    if (valid) {
+      uint4 *dst = reinterpret_cast<uint4 *>(dZ + row * kHid + c0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dst[q] = make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
+    }
+    if (to_act) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c0 + q * 8, kHid)) =
+            make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
+    }
+  };
+  // dz = D (from TMEM) * act'(z) for the row's stored pre-activations z.
+  auto through = [&](const __nv_bfloat16 *Z, __nv_bfloat16 *dZ, long long row, bool valid, bool to_act) {
+#pragma unroll 1
+    for (int c = 0; c < kHid / 32; ++c) {
+      uint32_t v[32];
+      tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
+      uint4 zr[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        zr[q] = valid ? __ldg(reinterpret_cast<const uint4 *>(Z + row * kHid + c * 32) + q) : make_uint4(0, 0, 0, 0);
+      tmem_wait_ld();
+      const uint32_t *zw = reinterpret_cast<const uint32_t *>(zr);
+      uint32_t d[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const float2 z = unpack_bf16(zw[i]);
+        d[i] = pack_bf16(__uint_as_float(v[2 * i]) * act_grad(z.x), __uint_as_float(v[2 * i + 1]) * act_grad(z.y));
+      }
+      put(dZ, row, valid, c * 32, d, to_act);
+    }
+  };
+
+  for (;;) {
+    if (lt == 0) s.item[g] = (int)atomicAdd(A.next, 1u);
+    named_sync(bar_id, kTcGroupThreads);
+    const int tile = s.item[g]; // rewritten only after the group's end-of-tile barrier below
+    if (tile >= tiles) break;
+    const long long row = (long long)tile * kTcGroupThreads + lt;
+    const bool valid = row < A.rows;
+    // dz3 = dy * w4 * act'(z3)
+    {
+      const float dy = valid ? A.dy[row] : 0.f;
+#pragma unroll 1
+      for (int c = 0; c < kHid / 32; ++c) {
+        uint4 zr[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          zr[q] = valid ? __ldg(reinterpret_cast<const uint4 *>(A.Z3 + row * kHid + c * 32) + q) : make_uint4(0, 0, 0, 0);
+        const uint32_t *zw = reinterpret_cast<const uint32_t *>(zr);
+        uint32_t d[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const float2 z = unpack_bf16(zw[i]);
+          const int f = c * 32 + 2 * i;
+          d[i] = pack_bf16(dy * s.w4f[f] * act_grad(z.x), dy * s.w4f[f + 1] * act_grad(z.y));
+        }
+        put(A.dZ3, row, valid, c * 32, d, true);
+      }
+    }
+    product(smem_u32(s.w3t));
+    through(A.Z2, A.dZ2, row, valid, true);
+    product(smem_u32(s.w2t));
+    through(A.Z1, A.dZ1, row, valid, false);
+    tc_fence_before();
     if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
       failed = true;
       break;

@@ -503,17 +503,18 @@ int screen_run(Context &c, const bude_screen_cfg &sc, bude_screen_stats *stats) 
     }
   }
   cudaEventRecord(ev[2], c.stream);
-  cudaError_t e = cudaStreamSynchronize(c.stream);
-  if (rc) return rc;
-  if (e != cudaSuccess) return cuda_error(e, "screen rescoring");
-  // 4. audit and fallback
+  if (rc) {
+    cudaStreamSynchronize(c.stream);
+    return rc;
+  }
+  // 4. audit and fallback (the audit follows the rescoring on the stream; one wait for both)
   if (nl > 0)
     audit_kernel<<<nl, 256, 0, c.stream>>>(s.comp_off.as<long long>(), s.counts.as<int>(), s.comp_pose.as<int>(),
                                            s.comp_exact.as<float>(), scores, s.err.as<float>());
   c.launches += nl > 0;
   std::vector<float> err((size_t)nl);
   if (nl > 0) cudaMemcpyAsync(err.data(), s.err.ptr, (size_t)nl * 4, cudaMemcpyDeviceToHost, c.stream);
-  e = cudaStreamSynchronize(c.stream);
+  cudaError_t e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return cuda_error(e, "screen audit");
   std::vector<int> fb_lig, fb_cnt;
   std::vector<long long> fb_first;

@@ -129,20 +129,13 @@ static int set_smem_limits() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(score_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem<3>));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(train_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(train_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(BwdSmem));
-  // Two backward blocks per SM (launch bounds cap the registers at 128): the shared-memory
-  // carveout must hold both.
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(train_backward_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared);
-  if (e == cudaSuccess)
     e = cudaFuncSetAttribute(wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WgTcSmem));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(train_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(TcSmem<kTcGroups>));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(train_backward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(TcBwdSmem<kTcGroups>));
   if (e != cudaSuccess) return cuda_error(e, "surrogate shared-memory limits");
   done = true;
   return BUDE_OK;
@@ -353,8 +346,6 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   m.lig_n = s.pose_lig_n.as<int>();
   m.nposes = nb;
   const MlpWeights W = weights(s);
-  const int tiles = (int)((rows + kRowsPerCta - 1) / kRowsPerCta);
-  const int nblk = std::min(tiles, 2 * std::max(c.num_sms, 1));
   // One gradient block per SM, each with at least one 128-row tile.
   const int wg_grid = (int)std::min<long long>((rows + kWgTile - 1) / kWgTile, std::max(c.num_sms, 1));
   int rc = ensure_train_scratch(s, rows, nb, wg_grid);
@@ -384,19 +375,27 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   train_loss_kernel<<<(nb + 127) / 128, 128, 0, c.stream>>>(m, s.y.as<float>(), p + kOffB4, s.labels.as<float>(),
                                                           s.pred.as<float>(), s.loss.as<float>(), s.dy.as<float>(),
                                                           s.dsum.as<float>(), 1.f / (float)nb);
-  BwdArgs b;
-  b.w2t = s.w2t_bf.as<__nv_bfloat16>();
-  b.w3t = s.w3t_bf.as<__nv_bfloat16>();
-  b.w4 = p + kOffW4;
-  b.Z1 = s.Z1.as<__nv_bfloat16>();
-  b.Z2 = s.Z2.as<__nv_bfloat16>();
-  b.Z3 = s.Z3.as<__nv_bfloat16>();
-  b.dy = s.dy.as<float>();
-  b.rows = (int)rows;
-  b.dZ1 = s.dZ1.as<__nv_bfloat16>();
-  b.dZ2 = s.dZ2.as<__nv_bfloat16>();
-  b.dZ3 = s.dZ3.as<__nv_bfloat16>();
-  train_backward_kernel<<<nblk, kMlpThreads, sizeof(BwdSmem), c.stream>>>(b);
+  {
+    // Backward through the hidden layers on the tensor cores (score_tc.cuh): dz3, dz2, dz1 as BF16.
+    cudaMemsetAsync(s.next.ptr, 0, sizeof(unsigned int), c.stream);
+    TrainBwdTcArgs b;
+    b.w3t = s.w3t_bf.as<__nv_bfloat16>();
+    b.w2t = s.w2t_bf.as<__nv_bfloat16>();
+    b.w4 = p + kOffW4;
+    b.Z1 = s.Z1.as<__nv_bfloat16>();
+    b.Z2 = s.Z2.as<__nv_bfloat16>();
+    b.Z3 = s.Z3.as<__nv_bfloat16>();
+    b.dy = s.dy.as<float>();
+    b.rows = (int)rows;
+    b.dZ1 = s.dZ1.as<__nv_bfloat16>();
+    b.dZ2 = s.dZ2.as<__nv_bfloat16>();
+    b.dZ3 = s.dZ3.as<__nv_bfloat16>();
+    b.err = c.err.as<unsigned int>();
+    b.next = s.next.as<unsigned int>();
+    const int btiles = (int)((rows + kTcGroupThreads - 1) / kTcGroupThreads);
+    const int grid = std::max(1, std::min((btiles + kTcGroups - 1) / kTcGroups, std::max(c.num_sms, 1)));
+    train_backward_tc_kernel<<<grid, kTcGroups * kTcGroupThreads, sizeof(TcBwdSmem<kTcGroups>), c.stream>>>(b);
+  }
   // Weight, bias and embedding gradients on the tensor cores (wgrad_tc.cuh): per-block partial
   // sums over contiguous row tiles, folded in block order.
   WgTcArgs w;
@@ -432,9 +431,8 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   reduce(part + kWgOffB1, wg_grid, kHid, kWgPart, gr + kOffB1);
   reduce(part + kWgOffW4, wg_grid, kHid, kWgPart, gr + kOffW4);
   reduce(part + kWgOffS, wg_grid, kHid * kMaxTypes, kWgPart, s.S_sum.as<float>());
-  reduce(s.dsum.as<float>(), nb, 1, 1, gr + kOffB4);
-  reduce_segments_kernel<<<(unsigned)(((long long)red.first[red.nseg] * kReduceLanes + 255) / 256), 256, 0,
-                           c.stream>>>(red);
+  reduce(s.dsum.as<float>(), (nb + 127) / 128, 1, 1, gr + kOffB4);
+  reduce_segments_kernel<<<(unsigned)((red.first[red.nseg] + 31) / 32), 32 * kReduceWarps, 0, c.stream>>>(red);
   emb_grad_kernel<<<(kMaxTypes * kEmb + 255) / 256, 256, 0, c.stream>>>(s.S_sum.as<float>(),
                                                                        s.w1_bf.as<__nv_bfloat16>(), gr + kOffEmb);
   if (lr > 0.f) {

@@ -391,182 +391,47 @@ __global__ void __launch_bounds__(256) train_features_kernel(MlpWeights W, Field
   }
 }
 
-// Forward over rows: saves z1, z2, z3 (BF16, [rows][128]) and y per row.
-__global__ void __launch_bounds__(kMlpThreads) train_forward_kernel(MlpWeights W, const __nv_bfloat16 *X, int rows,
-                                                                    __nv_bfloat16 *Z1, __nv_bfloat16 *Z2,
-                                                                    __nv_bfloat16 *Z3, float *y) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  MlpSmem &s = *reinterpret_cast<MlpSmem *>(smem_raw);
-  load_weights(s, W);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  for (int tile = blockIdx.x; tile * kRowsPerCta < rows; tile += gridDim.x) {
-    const int base = tile * kRowsPerCta;
-    __syncthreads();
-    for (int i = threadIdx.x; i < kRowsPerCta * kFeat / 8; i += blockDim.x) {
-      const int r = i / (kFeat / 8), k8 = i % (kFeat / 8);
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (base + r < rows) v = *reinterpret_cast<const uint4 *>(X + (long long)(base + r) * kFeat + k8 * 8);
-      *reinterpret_cast<uint4 *>(&s.x[r * kLdX + k8 * 8]) = v;
-    }
-    __syncthreads();
-    uint32_t ax[2][4], h[8][4], z[16][2];
-    float acc[16][4];
-    const int r0 = base + warp * 16 + g, r1 = r0 + 8;
-    auto store_z = [&](__nv_bfloat16 *Z) {
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        if (r0 < rows) *reinterpret_cast<uint32_t *>(Z + (long long)r0 * kHid + j * 8 + 2 * t) = z[j][0];
-        if (r1 < rows) *reinterpret_cast<uint32_t *>(Z + (long long)r1 * kHid + j * 8 + 2 * t) = z[j][1];
-      }
-    };
-    x_frags(s.x, warp * 16, ax);
-    layer_mma<2, kLdX>(acc, ax, s.w1);
-    act_to_frags(acc, s.b1, h, z);
-    store_z(Z1);
-    layer_mma<8, kLdH>(acc, h, s.w2);
-    act_to_frags(acc, s.b2, h, z);
-    store_z(Z2);
-    layer_mma<8, kLdH>(acc, h, s.w3);
-    act_to_frags(acc, s.b3, h, z);
-    store_z(Z3);
-    const float2 yy = last_layer(h, s.w4);
-    if (t == 0) {
-      if (r0 < rows) y[r0] = yy.x;
-      if (r1 < rows) y[r1] = yy.y;
-    }
-  }
-}
-
 // Per batch pose: prediction = sum of its rows' y + natlig * b4; loss on the compressed scale
 // c(E) = S * asinh(E / S); dy (per row) = dLoss/dprediction.  loss_out[i] = the pose's squared
-// error (summed on the host, deterministic); dsum[i] = the sum of dy over the pose's rows.
+// error (summed on the host, deterministic); dsum[block] = the sum of dy over the block's rows.
 constexpr float kLossScale = 20.f;
 
-__global__ void train_loss_kernel(RowMap m, const float *y, const float *b4, const float *labels, float *pred,
-                                  float *loss_out, float *dy, float *dsum, float inv_batch) {
+__global__ void __launch_bounds__(128) train_loss_kernel(RowMap m, const float *y, const float *b4,
+                                                         const float *labels, float *pred, float *loss_out, float *dy,
+                                                         float *dsum, float inv_batch) {
+  __shared__ float share[128];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m.nposes) return;
-  const int p = m.pose[i];
-  const int row0 = m.row_off[i], n = m.row_off[i + 1] - row0;
-  float s = 0.f;
-  for (int a = 0; a < n; ++a) s += y[row0 + a];
-  s += n * b4[0];
-  pred[i] = s;
-  const float cs = kLossScale * asinhf(s / kLossScale), ce = kLossScale * asinhf(labels[p] / kLossScale);
-  const float d = cs - ce;
-  loss_out[i] = d * d;
-  const float grad = 2.f * d * rsqrtf(1.f + (s / kLossScale) * (s / kLossScale)) * inv_batch;
-  for (int a = 0; a < n; ++a) dy[row0 + a] = grad;
-  dsum[i] = (float)n * grad; // the pose's share of the b4 gradient (sum of dy over its rows)
-}
-
-// Backward through the layers for a tile of rows: dz3 = dy * w4 * act'(z3), then
-// dz2 = (dz3 W3) * act'(z2) and dz1 = (dz2 W2) * act'(z1) on mma.sync, each stored as BF16 for the
-// gradient kernel (wgrad_tc.cuh), which also forms the bias, output-weight and embedding gradients.
-struct BwdArgs {
-  const __nv_bfloat16 *w2t; // [128][128]  (W2 transposed: in x out)
-  const __nv_bfloat16 *w3t; // [128][128]
-  const float *w4;
-  const __nv_bfloat16 *Z1, *Z2, *Z3;
-  const float *dy;
-  int rows;
-  __nv_bfloat16 *dZ1, *dZ2, *dZ3;
-};
-
-struct BwdSmem {
-  __nv_bfloat16 w2t[kHid * kLdH];
-  __nv_bfloat16 w3t[kHid * kLdH];
-  float w4[kHid];
-};
-
-__global__ void __launch_bounds__(kMlpThreads, 2) train_backward_kernel(BwdArgs a) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  BwdSmem &s = *reinterpret_cast<BwdSmem *>(smem_raw);
-  for (int i = threadIdx.x; i < kHid * kHid / 8; i += blockDim.x) {
-    const int o = i / (kHid / 8), k8 = i % (kHid / 8);
-    *reinterpret_cast<uint4 *>(&s.w2t[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(a.w2t) + i);
-    *reinterpret_cast<uint4 *>(&s.w3t[o * kLdH + k8 * 8]) = __ldg(reinterpret_cast<const uint4 *>(a.w3t) + i);
+  share[threadIdx.x] = 0.f;
+  if (i < m.nposes) {
+    const int p = m.pose[i];
+    const int row0 = m.row_off[i], n = m.row_off[i + 1] - row0;
+    float s = 0.f;
+    for (int a = 0; a < n; ++a) s += y[row0 + a];
+    s += n * b4[0];
+    pred[i] = s;
+    const float cs = kLossScale * asinhf(s / kLossScale), ce = kLossScale * asinhf(labels[p] / kLossScale);
+    const float d = cs - ce;
+    loss_out[i] = d * d;
+    const float grad = 2.f * d * rsqrtf(1.f + (s / kLossScale) * (s / kLossScale)) * inv_batch;
+    for (int a = 0; a < n; ++a) dy[row0 + a] = grad;
+    share[threadIdx.x] = (float)n * grad; // the pose's share of the b4 gradient (sum of dy over its rows)
   }
-  for (int i = threadIdx.x; i < kHid; i += blockDim.x) s.w4[i] = a.w4[i];
-  __syncthreads(); // the staged weights are read by every warp below
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-
-  for (int tile = blockIdx.x; tile * kRowsPerCta < a.rows; tile += gridDim.x) {
-    const int base = tile * kRowsPerCta;
-    const int r0 = base + warp * 16 + g, r1 = r0 + 8;
-    const bool v0 = r0 < a.rows, v1 = r1 < a.rows;
-    const float dy0 = v0 ? a.dy[r0] : 0.f, dy1 = v1 ? a.dy[r1] : 0.f;
-    auto zload = [&](const __nv_bfloat16 *Z, int j, float (&z)[4]) {
-      const float2 lo = v0 ? unpack_bf16(*reinterpret_cast<const uint32_t *>(Z + (long long)r0 * kHid + j * 8 + 2 * t))
-                           : make_float2(0.f, 0.f);
-      const float2 hi = v1 ? unpack_bf16(*reinterpret_cast<const uint32_t *>(Z + (long long)r1 * kHid + j * 8 + 2 * t))
-                           : make_float2(0.f, 0.f);
-      z[0] = lo.x; z[1] = lo.y; z[2] = hi.x; z[3] = hi.y;
-    };
-    auto dz_store = [&](__nv_bfloat16 *dZ, int j, const float (&d)[4]) {
-      if (v0) *reinterpret_cast<uint32_t *>(dZ + (long long)r0 * kHid + j * 8 + 2 * t) = pack_bf16(d[0], d[1]);
-      if (v1) *reinterpret_cast<uint32_t *>(dZ + (long long)r1 * kHid + j * 8 + 2 * t) = pack_bf16(d[2], d[3]);
-    };
-    // Layer 4 -> dz3.
-    float dz[16][4];
-    uint32_t A[8][4];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      float z[4];
-      zload(a.Z3, j, z);
-      const int c0 = j * 8 + 2 * t;
-      dz[j][0] = dy0 * s.w4[c0] * act_grad(z[0]);
-      dz[j][1] = dy0 * s.w4[c0 + 1] * act_grad(z[1]);
-      dz[j][2] = dy1 * s.w4[c0] * act_grad(z[2]);
-      dz[j][3] = dy1 * s.w4[c0 + 1] * act_grad(z[3]);
-    }
-    // dz -> BF16 A fragments of the next product, and stored.
-    auto to_frags = [&](const float (&d)[16][4], __nv_bfloat16 *dZ) {
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        dz_store(dZ, j, d[j]);
-        const uint32_t lo = pack_bf16(d[j][0], d[j][1]), hi = pack_bf16(d[j][2], d[j][3]);
-        if ((j & 1) == 0) {
-          A[j >> 1][0] = lo;
-          A[j >> 1][1] = hi;
-        } else {
-          A[j >> 1][2] = lo;
-          A[j >> 1][3] = hi;
-        }
-      }
-    };
-    to_frags(dz, a.dZ3);
-    // dh2 = dz3 W3 ; dz2 = dh2 * act'(z2)
-    float acc[16][4];
-    layer_mma<8, kLdH>(acc, A, s.w3t);
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      float z[4];
-      zload(a.Z2, j, z);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * act_grad(z[q]);
-    }
-    to_frags(dz, a.dZ2);
-    // dh1 = dz2 W2 ; dz1 = dh1 * act'(z1)
-    layer_mma<8, kLdH>(acc, A, s.w2t);
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      float z[4];
-      zload(a.Z1, j, z);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) dz[j][q] = acc[j][q] * act_grad(z[q]);
-    }
-#pragma unroll
-    for (int j = 0; j < 16; ++j) dz_store(a.dZ1, j, dz[j]);
+  // dsum[block] = the block's poses' shares, summed in a fixed tree order
+  __syncthreads();
+  for (int o = 64; o > 0; o >>= 1) {
+    if (threadIdx.x < o) share[threadIdx.x] += share[threadIdx.x + o];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) dsum[blockIdx.x] = share[0];
 }
 
 // The per-step gradient reductions in one launch: segment k sums parts [0, nparts) of
-// part[p * stride + i] into dst[i] for i < n.  Eight threads share an element: thread j adds parts
-// j, j + 8, j + 16, ... in order, then the eight sums are combined by a fixed butterfly, so the
-// result is the same bits on every run.
+// part[p * stride + i] into dst[i] for i < n.  A block of 8 warps takes 32 consecutive elements
+// (lane = element, so every load of a warp reads 32 consecutive floats); warp j adds parts
+// j, j + 8, j + 16, ... in order (eight loads in flight), and warp 0 adds the eight warps' sums in
+// warp order, so the result is the same bits on every run.
 constexpr int kMaxReduceSegs = 10;
-constexpr int kReduceLanes = 8;
+constexpr int kReduceWarps = 8;
 
 struct ReduceSegs {
   const float *part[kMaxReduceSegs];
@@ -578,22 +443,35 @@ struct ReduceSegs {
   int nseg;
 };
 
-__global__ void __launch_bounds__(256) reduce_segments_kernel(const ReduceSegs r) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int e = gt / kReduceLanes, j = gt % kReduceLanes;
+__global__ void __launch_bounds__(32 * kReduceWarps) reduce_segments_kernel(const ReduceSegs r) {
+  __shared__ float sums[kReduceWarps][32];
+  const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
+  const int e = blockIdx.x * 32 + lane;
   const bool live = e < r.first[r.nseg];
   int k = 0;
   while (live && k + 1 < r.nseg && r.first[k + 1] <= e) ++k;
   float v = 0.f;
   if (live) {
-    const int i = e - r.first[k];
-    const float *part = r.part[k] + i;
+    const float *part = r.part[k] + (e - r.first[k]);
     const long long stride = r.stride[k];
-    for (int p = j; p < r.nparts[k]; p += kReduceLanes) v += part[(long long)p * stride];
-  }
+    const int np = r.nparts[k];
+    int p = j;
+    for (; p + 7 * kReduceWarps < np; p += 8 * kReduceWarps) {
+      float x[8];
 #pragma unroll
-  for (int o = 1; o < kReduceLanes; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if (live && j == 0) r.dst[k][e - r.first[k]] = v;
+      for (int q = 0; q < 8; ++q) x[q] = part[(long long)(p + q * kReduceWarps) * stride];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v += x[q];
+    }
+    for (; p < np; p += kReduceWarps) v += part[(long long)p * stride];
+  }
+  sums[j][lane] = v;
+  __syncthreads();
+  if (j == 0 && live) {
+    float t = sums[0][lane];
+    for (int w = 1; w < kReduceWarps; ++w) t += sums[w][lane];
+    r.dst[k][e - r.first[k]] = t;
+  }
 }
 
 // Adam on the FP32 masters (Kingma & Ba, with the bias corrections applied as torch.optim.Adam

@@ -19,7 +19,8 @@
 // A block owns a contiguous range of 128-row tiles (the same on every run), so the partial sums
 // and their fixed-order reduction over blocks (reduce_segments_kernel) are deterministic.  Per
 // tile, phase A stages and issues layers 3 and 2, phase B layer 1 and the output weights, both in
-// one 136 KB region; a phase's UMMAs complete (bounded mbarrier wait) before the region is reused.
+// one 136 KB region; a phase's UMMAs complete (bounded mbarrier wait) before the region is reused,
+// and the next phase's global loads are in flight while they run.
 #pragma once
 #include <cstdint>
 
@@ -58,7 +59,7 @@ constexpr uint32_t kWgA1 = 0, kWgB1 = kWgA1 + wg_tile_bytes(kHid), kWgA4 = kWgB1
 constexpr uint32_t kWgRegion = kWgPhaseA > kWgPhaseB ? kWgPhaseA : kWgPhaseB;
 
 struct WgTcSmem {
-  alignas(1024) unsigned char region[kWgRegion];
+  alignas(128) unsigned char region[kWgRegion];
   alignas(8) uint64_t bar;
   uint32_t tmem;
 };
@@ -80,23 +81,27 @@ __device__ __forceinline__ void wg_put(unsigned char *tile, int nmn, int f0, int
   *reinterpret_cast<uint4 *>(tile + mnmajor_offset(f0, k, nmn)) = v;
 }
 
-// The 64 features [h*64, h*64+64) of row r of a [rows][128] BF16 array (zeros past the last row),
-// optionally through the activation.
-__device__ __forceinline__ void wg_load_half(const __nv_bfloat16 *src, long long r, bool valid, int h, bool apply_act,
-                                             uint4 (&v)[8]) {
+// The 64 features [h*64, h*64+64) of row r of a [rows][128] BF16 array (zeros past the last row).
+__device__ __forceinline__ void wg_load_half(const __nv_bfloat16 *src, long long r, bool valid, int h, uint4 (&v)[8]) {
 #pragma unroll
   for (int q = 0; q < 8; ++q)
     v[q] = valid ? __ldg(reinterpret_cast<const uint4 *>(src + r * kHid + h * 64) + q) : make_uint4(0, 0, 0, 0);
-  if (apply_act) {
+}
+
+// Store them as row k of an MN-major tile, optionally through the activation (BF16 in, BF16 out).
+__device__ __forceinline__ void wg_store_half(unsigned char *tile, int nmn, int h, int k, uint4 (&v)[8],
+                                              bool apply_act) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+  for (int q = 0; q < 8; ++q) {
+    if (apply_act) {
       uint32_t *w = reinterpret_cast<uint32_t *>(&v[q]);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const float2 f = unpack_bf16(w[e]);
-        w[e] = valid ? act_pair(f.x, f.y) : 0u;
+        w[e] = act_pair(f.x, f.y); // act(0) = 0: rows past the end stay zero
       }
     }
+    *reinterpret_cast<uint4 *>(tile + mnmajor_offset(h * 64 + q * 8, k, nmn)) = v[q];
   }
 }
 
@@ -106,7 +111,7 @@ __device__ __forceinline__ uint32_t wg_idesc(int n) {
 }
 
 __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs a) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   WgTcSmem &s = *reinterpret_cast<WgTcSmem *>(smem_raw);
   const int tid = threadIdx.x, r = tid % kWgTile, h = tid / kWgTile; // row of the tile, half
   const int tiles = (a.rows + kWgTile - 1) / kWgTile;
@@ -135,7 +140,8 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs 
       umma_bf16(tmem + col, umma_desc(base + a_off + kk * 2 * a_lbo, a_lbo, 128u),
                 umma_desc(base + b_off + kk * 2 * b_lbo, b_lbo, 128u), wg_idesc(nb), (first && kk == 0) ? 0u : 1u);
   };
-  auto issue_and_wait = [&](bool phase_a, bool first) {
+  // A phase's tiles are complete in shared memory: one thread issues its UMMAs and commits them.
+  auto issue = [&](bool phase_a, bool first) {
     fence_proxy_async();
     tc_fence_before();
     __syncthreads();
@@ -150,76 +156,89 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs 
       }
       umma_commit(&s.bar);
     }
+  };
+  // The phase's UMMAs have read the region (bounded wait), so it may be rewritten.
+  auto wait = [&]() {
     if (!mbar_wait_bounded(&s.bar, phase)) failed = true;
     phase ^= 1u;
     tc_fence_after();
   };
 
+  // Phase A's loads for a tile (all 32 16-byte loads in flight at once), then per tile: store A,
+  // issue A's UMMAs, load phase B while they run, store B once they are done, issue B's UMMAs,
+  // load the next tile's phase A while those run.
+  uint4 ad3[8], az2[8], ad2[8], az1[8];
+  auto load_a = [&](int tile) {
+    const long long row = (long long)tile * kWgTile + r;
+    const bool valid = row < a.rows;
+    wg_load_half(a.dZ3, row, valid, h, ad3);
+    wg_load_half(a.Z2, row, valid, h, az2);
+    wg_load_half(a.dZ2, row, valid, h, ad2);
+    wg_load_half(a.Z1, row, valid, h, az1);
+  };
+  if (t0 < t1) load_a(t0);
   for (int tile = t0; tile < t1; ++tile) {
     const long long row = (long long)tile * kWgTile + r;
     const bool valid = row < a.rows;
     const bool first = tile == t0;
     // Phase A: layers 3 and 2.
+    wg_store_half(R + kWgA3, kHid, h, r, ad3, false);
+    wg_store_half(R + kWgB3, kWgN3, h, r, az2, true);
+    wg_store_half(R + kWgA2, kHid, h, r, ad2, false);
+    wg_store_half(R + kWgB2, kWgN3, h, r, az1, true);
     {
-      uint4 v[8];
-      wg_load_half(a.dZ3, row, valid, h, false, v);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) wg_put(R + kWgA3, kHid, h * 64 + q * 8, r, v[q]);
-      wg_load_half(a.Z2, row, valid, h, true, v);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) wg_put(R + kWgB3, kWgN3, h * 64 + q * 8, r, v[q]);
-      wg_load_half(a.dZ2, row, valid, h, false, v);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) wg_put(R + kWgA2, kHid, h * 64 + q * 8, r, v[q]);
-      wg_load_half(a.Z1, row, valid, h, true, v);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) wg_put(R + kWgB2, kWgN3, h * 64 + q * 8, r, v[q]);
       // The bias column (a one per valid row) and 15 zero columns of both B tiles.
       const uint4 ones = (h == 0 && valid) ? one_first : make_uint4(0, 0, 0, 0);
       wg_put(R + kWgB3, kWgN3, kHid + h * 8, r, ones);
       wg_put(R + kWgB2, kWgN3, kHid + h * 8, r, ones);
     }
-    issue_and_wait(true, first);
-    if (__syncthreads_or(failed)) break;
-    // Phase B: layer 1 (with the one-hot types and the bias column) and the output weights.
-    {
-      uint4 v[8];
-      wg_load_half(a.dZ1, row, valid, h, false, v);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) wg_put(R + kWgA1, kHid, h * 64 + q * 8, r, v[q]);
-      wg_load_half(a.Z3, row, valid, h, true, v);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) wg_put(R + kWgA4, kHid, h * 64 + q * 8, r, v[q]);
+    issue(true, first);
+    // Phase B's loads while phase A's UMMAs run.
+    uint4 bd1[8], bz3[8], bx[4] = {};
+    int type = -1;
+    float d = 0.f;
+    wg_load_half(a.dZ1, row, valid, h, bd1);
+    wg_load_half(a.Z3, row, valid, h, bz3);
+    if (valid) {
       if (h == 0) {
-        // X (32 features), the bias column chunk, and dy as two BF16 parts
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint4 x = valid ? __ldg(reinterpret_cast<const uint4 *>(a.X + row * kFeat) + q) : make_uint4(0, 0, 0, 0);
-          wg_put(R + kWgB1, kWgN1, q * 8, r, x);
-        }
-        wg_put(R + kWgB1, kWgN1, kFeat + kMaxTypes, r, valid ? one_first : make_uint4(0, 0, 0, 0));
-        const float d = valid ? a.dy[row] : 0.f;
-        const __nv_bfloat16 hi = __float2bfloat16_rn(d);
-        const __nv_bfloat16 lo = __float2bfloat16_rn(d - __bfloat162float(hi));
-        const uint32_t db = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
-        wg_put(R + kWgB4, kWgN4, 0, r, make_uint4(db, 0u, 0u, 0u));
+        for (int q = 0; q < 4; ++q) bx[q] = __ldg(reinterpret_cast<const uint4 *>(a.X + row * kFeat) + q);
+        d = a.dy[row];
       } else {
-        // one-hot of the row's type (8 chunks) and the zero chunks
-        const int t = valid ? a.row_type[row] : -1;
-#pragma unroll
-        for (int q = 0; q < kMaxTypes / 8; ++q) {
-          uint4 c = make_uint4(0, 0, 0, 0);
-          if (t >= q * 8 && t < q * 8 + 8) {
-            uint32_t *w = reinterpret_cast<uint32_t *>(&c);
-            w[(t - q * 8) >> 1] = ((t - q * 8) & 1) ? 0x3F800000u : 0x3F80u;
-          }
-          wg_put(R + kWgB1, kWgN1, kFeat + q * 8, r, c);
-        }
-        wg_put(R + kWgB1, kWgN1, kFeat + kMaxTypes + 8, r, make_uint4(0, 0, 0, 0));
-        wg_put(R + kWgB4, kWgN4, 8, r, make_uint4(0, 0, 0, 0));
+        type = a.row_type[row];
       }
     }
-    issue_and_wait(false, first);
+    wait();
+    if (__syncthreads_or(failed)) break;
+    // Phase B: layer 1 (with the one-hot types and the bias column) and the output weights.
+    wg_store_half(R + kWgA1, kHid, h, r, bd1, false);
+    wg_store_half(R + kWgA4, kHid, h, r, bz3, true);
+    if (h == 0) {
+      // X (32 features), the bias column chunk, and dy as two BF16 parts
+#pragma unroll
+      for (int q = 0; q < 4; ++q) wg_put(R + kWgB1, kWgN1, q * 8, r, bx[q]);
+      wg_put(R + kWgB1, kWgN1, kFeat + kMaxTypes, r, valid ? one_first : make_uint4(0, 0, 0, 0));
+      const __nv_bfloat16 hi = __float2bfloat16_rn(d);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(d - __bfloat162float(hi));
+      const uint32_t db = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
+      wg_put(R + kWgB4, kWgN4, 0, r, make_uint4(db, 0u, 0u, 0u));
+    } else {
+      // one-hot of the row's type (8 chunks) and the zero chunks
+#pragma unroll
+      for (int q = 0; q < kMaxTypes / 8; ++q) {
+        uint4 c = make_uint4(0, 0, 0, 0);
+        if (type >= q * 8 && type < q * 8 + 8) {
+          uint32_t *w = reinterpret_cast<uint32_t *>(&c);
+          w[(type - q * 8) >> 1] = ((type - q * 8) & 1) ? 0x3F800000u : 0x3F80u;
+        }
+        wg_put(R + kWgB1, kWgN1, kFeat + q * 8, r, c);
+      }
+      wg_put(R + kWgB1, kWgN1, kFeat + kMaxTypes + 8, r, make_uint4(0, 0, 0, 0));
+      wg_put(R + kWgB4, kWgN4, 8, r, make_uint4(0, 0, 0, 0));
+    }
+    issue(false, first);
+    if (tile + 1 < t1) load_a(tile + 1);
+    wait();
     if (__syncthreads_or(failed)) break;
   }
 
