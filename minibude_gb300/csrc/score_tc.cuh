@@ -255,15 +255,15 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
 // ---------------------------------------------------------------------------------------------
 // Training forward pass on the same machinery: 128-row tiles of the step's (pose, ligand atom)
 // feature rows X instead of poses.  Per tile a group runs layers 1..3 as above and, after each,
-// stores the row's pre-activations z_l as BF16 ([rows][128], the backward pass and the gradient
-// kernel read them) before the activation goes back into `act`; the output layer gives y per row
+// stores the row's pre-activations z_l as BF16 (row-tiled, tc.cuh: tiled_offset; the backward
+// pass and the gradient kernel read them) before the activation goes back into `act`; the output layer gives y per row
 // (w4 . h3, without b4: the loss kernel adds natlig * b4 per pose).  Tiles come from a work
 // counter; a row's arithmetic does not depend on which group runs it.
 struct TrainFwdTcArgs {
   MlpWeights W;
-  const __nv_bfloat16 *X; // [rows][32]
+  const __nv_bfloat16 *X; // [rows][32], row-tiled
   int rows;
-  __nv_bfloat16 *Z1, *Z2, *Z3;
+  __nv_bfloat16 *Z1, *Z2, *Z3; // [tiled_rows(rows)][128], row-tiled
   float *y;
   unsigned int *err;
   unsigned int *next; // work counter, zero at launch
@@ -326,10 +326,14 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
         zb[i] = pack_bf16(z0, z1);
         hb[i] = act_pair(z0, z1);
       }
-      if (valid) {
-        uint4 *dst = reinterpret_cast<uint4 *>(Z + row * kHid + c * 32);
+      {
+        // Every row of the tile (rows past the end hold the bias pre-activations: finite, and
+        // their gradients are zero), so each warp store fills whole 128-byte lines.
+        unsigned char *zt = reinterpret_cast<unsigned char *>(Z) + tiled_offset(row, 0, kHid);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) dst[q] = make_uint4(zb[4 * q], zb[4 * q + 1], zb[4 * q + 2], zb[4 * q + 3]);
+        for (int q = 0; q < 4; ++q)
+          *reinterpret_cast<uint4 *>(zt + kmajor_offset(0, c * 32 + q * 8, kHid)) =
+              make_uint4(zb[4 * q], zb[4 * q + 1], zb[4 * q + 2], zb[4 * q + 3]);
       }
       if (to_act) {
 #pragma unroll
@@ -358,10 +362,13 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
     if (tile >= tiles) break;
     const long long row = (long long)tile * kTcGroupThreads + lt;
     const bool valid = row < A.rows;
-    const uint4 *x = reinterpret_cast<const uint4 *>(A.X + row * kFeat);
+    // The feature tile is the layer-1 operand tile byte for byte; rows past the end are zero.
+    const unsigned char *x = reinterpret_cast<const unsigned char *>(A.X) + (long long)tile * (kTcGroupThreads * kFeat * 2);
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, q * 8, kFeat)) = valid ? __ldg(x + q) : make_uint4(0, 0, 0, 0);
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t o = kmajor_offset(lt, q * 8, kFeat);
+      *reinterpret_cast<uint4 *>(act + o) = valid ? __ldg(reinterpret_cast<const uint4 *>(x + o)) : make_uint4(0, 0, 0, 0);
+    }
     fence_proxy_async();
     tc_fence_before();
     if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
@@ -394,8 +401,9 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
 //   dz3 = dy * w4 * act'(z3)                       (FMA pipe, from the stored z3 and dy)
 //   dz2 = (dz3 W3) * act'(z2),  dz1 = (dz2 W2) * act'(z1)   (UMMAs against the transposed weight
 //                                                   copies W3^T, W2^T, FP32 accumulators in TMEM)
-// Each dz is rounded to BF16, stored ([rows][128], the gradient kernel of wgrad_tc.cuh reads them)
-// and written into `act` as the next UMMA's A operand.
+// Each dz is rounded to BF16, stored (row-tiled, the gradient kernel of wgrad_tc.cuh reads them)
+// and written into `act` as the next UMMA's A operand.  Rows past the end have dy = 0, so their
+// dz are exactly zero.
 template <int G> struct TcBwdSmem {
   alignas(128) unsigned char w3t[kHid * kHid * 2]; // W3^T: [in 128][out 128], K-major (K = out)
   alignas(128) unsigned char w2t[kHid * kHid * 2]; // W2^T
@@ -410,10 +418,10 @@ static_assert(sizeof(TcBwdSmem<4>) <= 227 * 1024, "one block per SM fits the 227
 struct TrainBwdTcArgs {
   const __nv_bfloat16 *w3t, *w2t; // [in][out] BF16 (the published transposed copies)
   const float *w4;
-  const __nv_bfloat16 *Z1, *Z2, *Z3;
-  const float *dy;
+  const __nv_bfloat16 *Z1, *Z2, *Z3; // row-tiled, as the forward pass stored them
+  const float *dy;                   // [rows]
   int rows;
-  __nv_bfloat16 *dZ1, *dZ2, *dZ3;
+  __nv_bfloat16 *dZ1, *dZ2, *dZ3;    // [tiled_rows(rows)][128], row-tiled
   unsigned int *err;
   unsigned int *next; // work counter, zero at launch
 };
@@ -467,11 +475,13 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
   };
   // 16 dz values (BF16 pairs) of columns [c0, c0 + 32) -> the row of dZ in global memory and,
   // when to_act, the `act` tile.
-  auto put = [&](__nv_bfloat16 *dZ, long long row, bool valid, int c0, const uint32_t (&d)[16], bool to_act) {
-    if (valid) {
-      uint4 *dst = reinterpret_cast<uint4 *>(dZ + row * kHid + c0);
+  auto put = [&](__nv_bfloat16 *dZ, long long row, int c0, const uint32_t (&d)[16], bool to_act) {
+    {
+      unsigned char *dt = reinterpret_cast<unsigned char *>(dZ) + tiled_offset(row, 0, kHid);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) dst[q] = make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
+      for (int q = 0; q < 4; ++q)
+        *reinterpret_cast<uint4 *>(dt + kmajor_offset(0, c0 + q * 8, kHid)) =
+            make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
     }
     if (to_act) {
 #pragma unroll
@@ -481,15 +491,19 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
     }
   };
   // dz = D (from TMEM) * act'(z) for the row's stored pre-activations z.
-  auto through = [&](const __nv_bfloat16 *Z, __nv_bfloat16 *dZ, long long row, bool valid, bool to_act) {
+  auto load_z = [&](const __nv_bfloat16 *Z, long long row, int c0, uint4 (&zr)[4]) {
+    const unsigned char *zt = reinterpret_cast<const unsigned char *>(Z) + tiled_offset(row, 0, kHid);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      zr[q] = __ldg(reinterpret_cast<const uint4 *>(zt + kmajor_offset(0, c0 + q * 8, kHid)));
+  };
+  auto through = [&](const __nv_bfloat16 *Z, __nv_bfloat16 *dZ, long long row, bool to_act) {
 #pragma unroll 1
     for (int c = 0; c < kHid / 32; ++c) {
       uint32_t v[32];
       tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
       uint4 zr[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        zr[q] = valid ? __ldg(reinterpret_cast<const uint4 *>(Z + row * kHid + c * 32) + q) : make_uint4(0, 0, 0, 0);
+      load_z(Z, row, c * 32, zr);
       tmem_wait_ld();
       const uint32_t *zw = reinterpret_cast<const uint32_t *>(zr);
       uint32_t d[16];
@@ -498,7 +512,7 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
         const float2 z = unpack_bf16(zw[i]);
         d[i] = pack_bf16(__uint_as_float(v[2 * i]) * act_grad(z.x), __uint_as_float(v[2 * i + 1]) * act_grad(z.y));
       }
-      put(dZ, row, valid, c * 32, d, to_act);
+      put(dZ, row, c * 32, d, to_act);
     }
   };
 
@@ -515,9 +529,7 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
 #pragma unroll 1
       for (int c = 0; c < kHid / 32; ++c) {
         uint4 zr[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-          zr[q] = valid ? __ldg(reinterpret_cast<const uint4 *>(A.Z3 + row * kHid + c * 32) + q) : make_uint4(0, 0, 0, 0);
+        load_z(A.Z3, row, c * 32, zr);
         const uint32_t *zw = reinterpret_cast<const uint32_t *>(zr);
         uint32_t d[16];
 #pragma unroll
@@ -526,13 +538,13 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
           const int f = c * 32 + 2 * i;
           d[i] = pack_bf16(dy * s.w4f[f] * act_grad(z.x), dy * s.w4f[f + 1] * act_grad(z.y));
         }
-        put(A.dZ3, row, valid, c * 32, d, true);
+        put(A.dZ3, row, c * 32, d, true);
       }
     }
     product(smem_u32(s.w3t));
-    through(A.Z2, A.dZ2, row, valid, true);
+    through(A.Z2, A.dZ2, row, true);
     product(smem_u32(s.w2t));
-    through(A.Z1, A.dZ1, row, valid, false);
+    through(A.Z1, A.dZ1, row, false);
     tc_fence_before();
     if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
       failed = true;

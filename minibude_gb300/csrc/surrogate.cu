@@ -316,7 +316,8 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
 static int ensure_train_scratch(Surrogate &s, long long rows, int batch, int wg_blocks) {
   int rc = BUDE_OK;
   if (rows > s.rows_cap) {
-    const size_t r = (size_t)rows;
+    // The row-tiled arrays (tc.cuh: tiled_offset) hold whole 128-row tiles.
+    const size_t r = (size_t)tiled_rows(rows);
     rc = s.X.reserve(r * kFeat * 2, "X");
     if (!rc) rc = s.row_type.reserve(r * 4, "row types");
     for (DevBuf *b : {&s.Z1, &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3})
@@ -324,7 +325,7 @@ static int ensure_train_scratch(Surrogate &s, long long rows, int batch, int wg_
     if (!rc) rc = s.y.reserve(r * 4, "y");
     if (!rc) rc = s.dy.reserve(r * 4, "dy");
     if (rc) return rc;
-    s.rows_cap = rows;
+    s.rows_cap = (long long)r;
   }
   if (!rc) rc = s.pred.reserve((size_t)batch * 4, "pred");
   if (!rc) rc = s.loss.reserve((size_t)batch * 4, "loss");
@@ -670,13 +671,14 @@ int surrogate_features(Context &c, const int *poses, int n, float *X, int *types
                                                                       s.X.as<__nv_bfloat16>(), s.row_type.as<int>());
   e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return cuda_error(e, "surrogate features");
-  std::vector<uint16_t> xb((size_t)rows * kFeat);
+  std::vector<uint16_t> xb((size_t)tiled_rows(rows) * kFeat);
   e = copy_sync(c, xb.data(), s.X.ptr, xb.size() * 2, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_error(e, "feature read-back");
-  for (size_t i = 0; i < xb.size(); ++i) {
-    const uint32_t u = (uint32_t)xb[i] << 16;
-    std::memcpy(&X[i], &u, 4);
-  }
+  for (long long r = 0; r < rows; ++r)
+    for (int k = 0; k < kFeat; ++k) {
+      const uint32_t u = (uint32_t)xb[(size_t)(tiled_offset(r, k, kFeat) / 2)] << 16;
+      std::memcpy(&X[(size_t)r * kFeat + k], &u, 4);
+    }
   if (types) e = copy_sync(c, types, s.row_type.ptr, (size_t)rows * 4, cudaMemcpyDeviceToHost);
   return e == cudaSuccess ? BUDE_OK : cuda_error(e, "row type read-back");
 }

@@ -34,6 +34,7 @@
 
 #include "mlp.cuh"
 #include "ptx.cuh"
+#include "tc.cuh"
 
 namespace bude {
 
@@ -369,7 +370,8 @@ struct RowMap {
   int nposes;
 };
 
-// One warp per batch pose writes the features (and types) of its rows.
+// One warp per batch pose writes the features (and types) of its rows; X is row-tiled (tc.cuh:
+// tiled_offset).
 __global__ void __launch_bounds__(256) train_features_kernel(MlpWeights W, FieldGrid g, const float4 *ligands,
                                                              const float4 *xform, RowMap m, __nv_bfloat16 *X,
                                                              int *row_type) {
@@ -382,11 +384,11 @@ __global__ void __launch_bounds__(256) train_features_kernel(MlpWeights W, Field
     const float4 la = __ldg(&ligands[first + a]);
     uint32_t f[kFeat / 2];
     atom_features(W, g, la, xform + (long long)p * 3, f);
-    uint4 *dst = reinterpret_cast<uint4 *>(X + (long long)(row0 + a) * kFeat);
-    dst[0] = make_uint4(f[0], f[1], f[2], f[3]);
-    dst[1] = make_uint4(f[4], f[5], f[6], f[7]);
-    dst[2] = make_uint4(f[8], f[9], f[10], f[11]);
-    dst[3] = make_uint4(f[12], f[13], f[14], f[15]);
+    unsigned char *xb = reinterpret_cast<unsigned char *>(X);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      *reinterpret_cast<uint4 *>(xb + tiled_offset(row0 + a, q * 8, kFeat)) =
+          make_uint4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
     row_type[row0 + a] = __float_as_int(la.w);
   }
 }

@@ -22,6 +22,15 @@ __host__ __device__ __forceinline__ uint32_t kmajor_offset(int m, int k, int kdi
   return (uint32_t)((m >> 3) * (kdim / 8) * 128 + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
 }
 
+// Row-tiled global layout of a [rows][kdim] BF16 array (the training pass's features,
+// pre-activations and their gradients): 128-row tiles of 128 * kdim * 2 contiguous bytes, each in
+// the K-major layout above, so a tile is byte for byte the shared-memory operand tile and the 16
+// bytes that 8 consecutive rows keep at the same k form one 128-byte line.  Byte offset of (row, k).
+__host__ __device__ __forceinline__ long long tiled_offset(long long row, int k, int kdim) {
+  return (row >> 7) * (128LL * kdim * 2) + kmajor_offset((int)(row & 127), k, kdim);
+}
+__host__ __device__ __forceinline__ long long tiled_rows(long long rows) { return (rows + 127) / 128 * 128; }
+
 // Shared-memory matrix descriptor (sm_100 format): start address, leading and stride byte
 // offsets (all >> 4), descriptor version 1 at bits 46-47, base offset 0, no swizzle (bits 61-63).
 __device__ __forceinline__ uint64_t umma_desc(uint32_t smem_addr, uint32_t lbo, uint32_t sbo) {

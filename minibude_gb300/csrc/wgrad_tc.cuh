@@ -66,10 +66,10 @@ struct WgTcSmem {
 static_assert(sizeof(WgTcSmem) <= 227 * 1024, "the staging region fits one block per SM");
 
 struct WgTcArgs {
-  const __nv_bfloat16 *X;                // [rows][32]
+  const __nv_bfloat16 *X;                // [rows][32], row-tiled (tc.cuh: tiled_offset)
   const int *row_type;                   // [rows]
-  const __nv_bfloat16 *Z1, *Z2, *Z3;     // [rows][128] pre-activations
-  const __nv_bfloat16 *dZ1, *dZ2, *dZ3;  // [rows][128]
+  const __nv_bfloat16 *Z1, *Z2, *Z3;     // [tiled_rows(rows)][128] pre-activations, row-tiled
+  const __nv_bfloat16 *dZ1, *dZ2, *dZ3;  // [tiled_rows(rows)][128], row-tiled; zero past the end
   const float *dy;                       // [rows]
   int rows;
   float *part;                           // [gridDim.x][kWgPart]
@@ -81,11 +81,12 @@ __device__ __forceinline__ void wg_put(unsigned char *tile, int nmn, int f0, int
   *reinterpret_cast<uint4 *>(tile + mnmajor_offset(f0, k, nmn)) = v;
 }
 
-// The 64 features [h*64, h*64+64) of row r of a [rows][128] BF16 array (zeros past the last row).
-__device__ __forceinline__ void wg_load_half(const __nv_bfloat16 *src, long long r, bool valid, int h, uint4 (&v)[8]) {
+// The 64 features [h*64, h*64+64) of row r of a row-tiled [rows][128] BF16 array (every row of a
+// tile is written: rows past the end have zero gradients and finite pre-activations).
+__device__ __forceinline__ void wg_load_half(const __nv_bfloat16 *src, long long r, int h, uint4 (&v)[8]) {
+  const unsigned char *t = reinterpret_cast<const unsigned char *>(src) + tiled_offset(r, 0, kHid);
 #pragma unroll
-  for (int q = 0; q < 8; ++q)
-    v[q] = valid ? __ldg(reinterpret_cast<const uint4 *>(src + r * kHid + h * 64) + q) : make_uint4(0, 0, 0, 0);
+  for (int q = 0; q < 8; ++q) v[q] = __ldg(reinterpret_cast<const uint4 *>(t + kmajor_offset(0, h * 64 + q * 8, kHid)));
 }
 
 // Store them as row k of an MN-major tile, optionally through the activation (BF16 in, BF16 out).
@@ -170,11 +171,10 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs 
   uint4 ad3[8], az2[8], ad2[8], az1[8];
   auto load_a = [&](int tile) {
     const long long row = (long long)tile * kWgTile + r;
-    const bool valid = row < a.rows;
-    wg_load_half(a.dZ3, row, valid, h, ad3);
-    wg_load_half(a.Z2, row, valid, h, az2);
-    wg_load_half(a.dZ2, row, valid, h, ad2);
-    wg_load_half(a.Z1, row, valid, h, az1);
+    wg_load_half(a.dZ3, row, h, ad3);
+    wg_load_half(a.Z2, row, h, az2);
+    wg_load_half(a.dZ2, row, h, ad2);
+    wg_load_half(a.Z1, row, h, az1);
   };
   if (t0 < t1) load_a(t0);
   for (int tile = t0; tile < t1; ++tile) {
@@ -197,12 +197,13 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs 
     uint4 bd1[8], bz3[8], bx[4] = {};
     int type = -1;
     float d = 0.f;
-    wg_load_half(a.dZ1, row, valid, h, bd1);
-    wg_load_half(a.Z3, row, valid, h, bz3);
+    wg_load_half(a.dZ1, row, h, bd1);
+    wg_load_half(a.Z3, row, h, bz3);
     if (valid) {
       if (h == 0) {
+        const unsigned char *xt = reinterpret_cast<const unsigned char *>(a.X) + tiled_offset(row, 0, kFeat);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) bx[q] = __ldg(reinterpret_cast<const uint4 *>(a.X + row * kFeat) + q);
+        for (int q = 0; q < 4; ++q) bx[q] = __ldg(reinterpret_cast<const uint4 *>(xt + kmajor_offset(0, q * 8, kFeat)));
         d = a.dy[row];
       } else {
         type = a.row_type[row];
