@@ -355,6 +355,7 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
     named_sync(bar_id, kTcGroupThreads);
   };
 
+  constexpr uint32_t kXTile = kTcGroupThreads * kFeat * 2;
   for (;;) {
     if (lt == 0) s.item[g] = (int)atomicAdd(A.next, 1u);
     named_sync(bar_id, kTcGroupThreads);
@@ -363,7 +364,7 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
     const long long row = (long long)tile * kTcGroupThreads + lt;
     const bool valid = row < A.rows;
     // The feature tile is the layer-1 operand tile byte for byte; rows past the end are zero.
-    const unsigned char *x = reinterpret_cast<const unsigned char *>(A.X) + (long long)tile * (kTcGroupThreads * kFeat * 2);
+    const unsigned char *x = reinterpret_cast<const unsigned char *>(A.X) + (long long)tile * kXTile;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const uint32_t o = kmajor_offset(lt, q * 8, kFeat);
@@ -403,7 +404,12 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
 //                                                   copies W3^T, W2^T, FP32 accumulators in TMEM)
 // Each dz is rounded to BF16, stored (row-tiled, the gradient kernel of wgrad_tc.cuh reads them)
 // and written into `act` as the next UMMA's A operand.  Rows past the end have dy = 0, so their
-// dz are exactly zero.
+// dz are exactly zero.  The pass streams the pre-activations once, so a thread keeps its row's
+// whole z_l (256 bytes) in registers: the 16 loads of a layer are in flight together, and those of
+// z2 and z1 are issued while the UMMA before them runs.  Three groups per block leave each thread
+// the registers for that (a fourth would cap it at 128).
+constexpr int kBwdGroups = 3;
+
 template <int G> struct TcBwdSmem {
   alignas(128) unsigned char w3t[kHid * kHid * 2]; // W3^T: [in 128][out 128], K-major (K = out)
   alignas(128) unsigned char w2t[kHid * kHid * 2]; // W2^T
@@ -413,7 +419,7 @@ template <int G> struct TcBwdSmem {
   int item[G];
   uint32_t tmem;
 };
-static_assert(sizeof(TcBwdSmem<4>) <= 227 * 1024, "one block per SM fits the 227 KB shared-memory limit");
+static_assert(sizeof(TcBwdSmem<kBwdGroups>) <= 227 * 1024, "one block per SM fits the 227 KB shared-memory limit");
 
 struct TrainBwdTcArgs {
   const __nv_bfloat16 *w3t, *w2t; // [in][out] BF16 (the published transposed copies)
@@ -426,8 +432,16 @@ struct TrainBwdTcArgs {
   unsigned int *next; // work counter, zero at launch
 };
 
-__global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward_tc_kernel(const TrainBwdTcArgs A) {
-  constexpr int G = kTcGroups;
+// Row `row`'s 128 BF16 values of a row-tiled [rows][128] array, as 16 chunks of 8 (all loads issued
+// before any is used).
+__device__ __forceinline__ void load_row128(const __nv_bfloat16 *src, long long row, uint4 (&v)[16]) {
+  const unsigned char *t = reinterpret_cast<const unsigned char *>(src) + tiled_offset(row, 0, kHid);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) v[q] = __ldg(reinterpret_cast<const uint4 *>(t + kmajor_offset(0, q * 8, kHid)));
+}
+
+__global__ void __launch_bounds__(kBwdGroups * kTcGroupThreads, 1) train_backward_tc_kernel(const TrainBwdTcArgs A) {
+  constexpr int G = kBwdGroups;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TcBwdSmem<G> &s = *reinterpret_cast<TcBwdSmem<G> *>(smem_raw);
   const int tid = threadIdx.x, g = tid / kTcGroupThreads, lt = tid % kTcGroupThreads;
@@ -456,8 +470,9 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
   bool failed = false;
   const int tiles = (A.rows + kTcGroupThreads - 1) / kTcGroupThreads;
 
-  // D = act * Wt^T over K = 128 (no bias), issued by the group's first thread, then waited for.
-  auto product = [&](uint32_t wt) {
+  // D = act * Wt^T over K = 128 (no bias), issued by the group's first thread once every thread's
+  // part of `act` is written; product_wait waits for it.
+  auto product_issue = [&](uint32_t wt) {
     fence_proxy_async();
     tc_fence_before();
     named_sync(bar_id, kTcGroupThreads);
@@ -469,6 +484,8 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
                   kk ? 1u : 0u);
       umma_commit(bar);
     }
+  };
+  auto product_wait = [&]() {
     if (!mbar_wait_sleep_bounded(bar, phase)) failed = true;
     phase ^= 1u;
     tc_fence_after();
@@ -476,13 +493,11 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
   // 16 dz values (BF16 pairs) of columns [c0, c0 + 32) -> the row of dZ in global memory and,
   // when to_act, the `act` tile.
   auto put = [&](__nv_bfloat16 *dZ, long long row, int c0, const uint32_t (&d)[16], bool to_act) {
-    {
-      unsigned char *dt = reinterpret_cast<unsigned char *>(dZ) + tiled_offset(row, 0, kHid);
+    unsigned char *dt = reinterpret_cast<unsigned char *>(dZ) + tiled_offset(row, 0, kHid);
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
-        *reinterpret_cast<uint4 *>(dt + kmajor_offset(0, c0 + q * 8, kHid)) =
-            make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
-    }
+    for (int q = 0; q < 4; ++q)
+      *reinterpret_cast<uint4 *>(dt + kmajor_offset(0, c0 + q * 8, kHid)) =
+          make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
     if (to_act) {
 #pragma unroll
       for (int q = 0; q < 4; ++q)
@@ -490,27 +505,19 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
             make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
     }
   };
-  // dz = D (from TMEM) * act'(z) for the row's stored pre-activations z.
-  auto load_z = [&](const __nv_bfloat16 *Z, long long row, int c0, uint4 (&zr)[4]) {
-    const unsigned char *zt = reinterpret_cast<const unsigned char *>(Z) + tiled_offset(row, 0, kHid);
+  // dz = D (from TMEM) * act'(z) for the row's pre-activations z (in registers).
+  auto through = [&](const uint4 (&z)[16], __nv_bfloat16 *dZ, long long row, bool to_act) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      zr[q] = __ldg(reinterpret_cast<const uint4 *>(zt + kmajor_offset(0, c0 + q * 8, kHid)));
-  };
-  auto through = [&](const __nv_bfloat16 *Z, __nv_bfloat16 *dZ, long long row, bool to_act) {
-#pragma unroll 1
     for (int c = 0; c < kHid / 32; ++c) {
       uint32_t v[32];
       tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
-      uint4 zr[4];
-      load_z(Z, row, c * 32, zr);
       tmem_wait_ld();
-      const uint32_t *zw = reinterpret_cast<const uint32_t *>(zr);
+      const uint32_t *zw = reinterpret_cast<const uint32_t *>(&z[4 * c]);
       uint32_t d[16];
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
-        const float2 z = unpack_bf16(zw[i]);
-        d[i] = pack_bf16(__uint_as_float(v[2 * i]) * act_grad(z.x), __uint_as_float(v[2 * i + 1]) * act_grad(z.y));
+        const float2 zz = unpack_bf16(zw[i]);
+        d[i] = pack_bf16(__uint_as_float(v[2 * i]) * act_grad(zz.x), __uint_as_float(v[2 * i + 1]) * act_grad(zz.y));
       }
       put(dZ, row, c * 32, d, to_act);
     }
@@ -523,28 +530,30 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_backward
     if (tile >= tiles) break;
     const long long row = (long long)tile * kTcGroupThreads + lt;
     const bool valid = row < A.rows;
+    uint4 z[16];
+    const float dy = valid ? A.dy[row] : 0.f;
+    load_row128(A.Z3, row, z);
     // dz3 = dy * w4 * act'(z3)
-    {
-      const float dy = valid ? A.dy[row] : 0.f;
-#pragma unroll 1
-      for (int c = 0; c < kHid / 32; ++c) {
-        uint4 zr[4];
-        load_z(A.Z3, row, c * 32, zr);
-        const uint32_t *zw = reinterpret_cast<const uint32_t *>(zr);
-        uint32_t d[16];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const float2 z = unpack_bf16(zw[i]);
-          const int f = c * 32 + 2 * i;
-          d[i] = pack_bf16(dy * s.w4f[f] * act_grad(z.x), dy * s.w4f[f + 1] * act_grad(z.y));
-        }
-        put(A.dZ3, row, c * 32, d, true);
+    for (int c = 0; c < kHid / 32; ++c) {
+      const uint32_t *zw = reinterpret_cast<const uint32_t *>(&z[4 * c]);
+      uint32_t d[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const float2 zz = unpack_bf16(zw[i]);
+        const int f = c * 32 + 2 * i;
+        d[i] = pack_bf16(dy * s.w4f[f] * act_grad(zz.x), dy * s.w4f[f + 1] * act_grad(zz.y));
       }
+      put(A.dZ3, row, c * 32, d, true);
     }
-    product(smem_u32(s.w3t));
-    through(A.Z2, A.dZ2, row, true);
-    product(smem_u32(s.w2t));
-    through(A.Z1, A.dZ1, row, false);
+    product_issue(smem_u32(s.w3t));
+    load_row128(A.Z2, row, z); // in flight while the UMMA runs
+    product_wait();
+    through(z, A.dZ2, row, true);
+    product_issue(smem_u32(s.w2t));
+    load_row128(A.Z1, row, z);
+    product_wait();
+    through(z, A.dZ1, row, false);
     tc_fence_before();
     if (named_sync_or(bar_id, kTcGroupThreads, failed)) {
       failed = true;

@@ -103,19 +103,28 @@ static MlpWeights weights(Surrogate &s) {
   return W;
 }
 
+// The BF16 copies of the weights (plain, and transposed for the backward pass).
+static BfCopies bf_copies(Surrogate &s) {
+  BfCopies c{};
+  auto add = [&](long long off, int rows, int cols, DevBuf *plain, DevBuf *trans) {
+    const int k = c.n++;
+    c.off[k] = off;
+    c.rows[k] = rows;
+    c.cols[k] = cols;
+    c.plain[k] = plain ? plain->as<__nv_bfloat16>() : nullptr;
+    c.trans[k] = trans ? trans->as<__nv_bfloat16>() : nullptr;
+  };
+  add(kOffEmb, kMaxTypes, kEmb, &s.emb_bf, nullptr);
+  add(kOffW1, kHid, kFeat, &s.w1_bf, &s.w1t_bf);
+  add(kOffW2, kHid, kHid, &s.w2_bf, &s.w2t_bf);
+  add(kOffW3, kHid, kHid, &s.w3_bf, &s.w3t_bf);
+  return c;
+}
+
 // Refresh the BF16 copies of the weights from the FP32 masters.
 static int publish(Context &c, Surrogate &s) {
-  const float *p = s.params.as<float>();
-  auto launch = [&](long long off, int rows, int cols, DevBuf *plain, DevBuf *trans) {
-    const int n = rows * cols;
-    publish_kernel<<<(n + 255) / 256, 256, 0, c.stream>>>(p + off, rows, cols,
-                                                          plain ? plain->as<__nv_bfloat16>() : nullptr,
-                                                          trans ? trans->as<__nv_bfloat16>() : nullptr);
-  };
-  launch(kOffEmb, kMaxTypes, kEmb, &s.emb_bf, nullptr);
-  launch(kOffW1, kHid, kFeat, &s.w1_bf, &s.w1t_bf);
-  launch(kOffW2, kHid, kHid, &s.w2_bf, &s.w2t_bf);
-  launch(kOffW3, kHid, kHid, &s.w3_bf, &s.w3t_bf);
+  publish_kernel<<<(unsigned)((kOffW3 + kHid * kHid + 255) / 256), 256, 0, c.stream>>>(s.params.as<float>(),
+                                                                                      kOffW3 + kHid * kHid, bf_copies(s));
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? BUDE_OK : cuda_error(e, "surrogate publish");
 }
@@ -135,7 +144,7 @@ static int set_smem_limits() {
                              (int)sizeof(TcSmem<kTcGroups>));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(train_backward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(TcBwdSmem<kTcGroups>));
+                             (int)sizeof(TcBwdSmem<kBwdGroups>));
   if (e != cudaSuccess) return cuda_error(e, "surrogate shared-memory limits");
   done = true;
   return BUDE_OK;
@@ -394,8 +403,8 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     b.err = c.err.as<unsigned int>();
     b.next = s.next.as<unsigned int>();
     const int btiles = (int)((rows + kTcGroupThreads - 1) / kTcGroupThreads);
-    const int grid = std::max(1, std::min((btiles + kTcGroups - 1) / kTcGroups, std::max(c.num_sms, 1)));
-    train_backward_tc_kernel<<<grid, kTcGroups * kTcGroupThreads, sizeof(TcBwdSmem<kTcGroups>), c.stream>>>(b);
+    const int grid = std::max(1, std::min((btiles + kBwdGroups - 1) / kBwdGroups, std::max(c.num_sms, 1)));
+    train_backward_tc_kernel<<<grid, kBwdGroups * kTcGroupThreads, sizeof(TcBwdSmem<kBwdGroups>), c.stream>>>(b);
   }
   // Weight, bias and embedding gradients on the tensor cores (wgrad_tc.cuh): per-block partial
   // sums over contiguous row tiles, folded in block order.
@@ -434,7 +443,7 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   reduce(part + kWgOffS, wg_grid, kHid * kMaxTypes, kWgPart, s.S_sum.as<float>());
   reduce(s.dsum.as<float>(), (nb + 127) / 128, 1, 1, gr + kOffB4);
   reduce_segments_kernel<<<(unsigned)((red.first[red.nseg] + 31) / 32), 32 * kReduceWarps, 0, c.stream>>>(red);
-  emb_grad_kernel<<<(kMaxTypes * kEmb + 255) / 256, 256, 0, c.stream>>>(s.S_sum.as<float>(),
+  emb_grad_kernel<<<(kMaxTypes * kEmb * 32 + 255) / 256, 256, 0, c.stream>>>(s.S_sum.as<float>(),
                                                                        s.w1_bf.as<__nv_bfloat16>(), gr + kOffEmb);
   if (lr > 0.f) {
     s.step++;
@@ -442,9 +451,7 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     const double bc1 = 1.0 - std::pow((double)b1, (double)s.step), bc2 = 1.0 - std::pow((double)b2, (double)s.step);
     adam_kernel<<<(unsigned)((kNParams + 255) / 256), 256, 0, c.stream>>>(
         s.params.as<float>(), s.adam_m.as<float>(), s.adam_v.as<float>(), gr, kNParams, (float)(lr / bc1),
-        (float)std::sqrt(bc2), b1, b2, 1e-8f);
-    rc = publish(c, s);
-    if (rc) return rc;
+        (float)std::sqrt(bc2), b1, b2, 1e-8f, bf_copies(s));
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "surrogate training step");

@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(128) train_loss_kernel(RowMap m, const float *
 // The per-step gradient reductions in one launch: segment k sums parts [0, nparts) of
 // part[p * stride + i] into dst[i] for i < n.  A block of 8 warps takes 32 consecutive elements
 // (lane = element, so every load of a warp reads 32 consecutive floats); warp j adds parts
-// j, j + 8, j + 16, ... in order (eight loads in flight), and warp 0 adds the eight warps' sums in
+// j, j + 8, j + 16, ... in order (24 loads in flight), and warp 0 adds the eight warps' sums in
 // warp order, so the result is the same bits on every run.
 constexpr int kMaxReduceSegs = 10;
 constexpr int kReduceWarps = 8;
@@ -457,15 +457,14 @@ __global__ void __launch_bounds__(32 * kReduceWarps) reduce_segments_kernel(cons
     const float *part = r.part[k] + (e - r.first[k]);
     const long long stride = r.stride[k];
     const int np = r.nparts[k];
-    int p = j;
-    for (; p + 7 * kReduceWarps < np; p += 8 * kReduceWarps) {
-      float x[8];
+    // 24 parts per round, all loads in flight at once (a part past the end adds +0).
+    for (int p = j; p < np; p += 24 * kReduceWarps) {
+      float x[24];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) x[q] = part[(long long)(p + q * kReduceWarps) * stride];
+      for (int q = 0; q < 24; ++q) x[q] = p + q * kReduceWarps < np ? part[(long long)(p + q * kReduceWarps) * stride] : 0.f;
 #pragma unroll
-      for (int q = 0; q < 8; ++q) v += x[q];
+      for (int q = 0; q < 24; ++q) v += x[q];
     }
-    for (; p < np; p += kReduceWarps) v += part[(long long)p * stride];
   }
   sums[j][lane] = v;
   __syncthreads();
@@ -476,12 +475,35 @@ __global__ void __launch_bounds__(32 * kReduceWarps) reduce_segments_kernel(cons
   }
 }
 
+// BF16 copies of FP32 master matrices inside the parameter vector: matrix k is the [rows][cols]
+// block at off[k], copied plainly and/or transposed (null pointers skip a copy).
+struct BfCopies {
+  long long off[4];
+  int rows[4], cols[4];
+  __nv_bfloat16 *plain[4], *trans[4];
+  int n;
+};
+
+__device__ __forceinline__ void bf_copy(const BfCopies &c, long long i, float w) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const long long j = i - c.off[k];
+    if (k < c.n && j >= 0 && j < (long long)c.rows[k] * c.cols[k]) {
+      const int r = (int)(j / c.cols[k]), col = (int)(j % c.cols[k]);
+      const __nv_bfloat16 b = __float2bfloat16_rn(w);
+      if (c.plain[k]) c.plain[k][j] = b;
+      if (c.trans[k]) c.trans[k][(long long)col * c.rows[k] + r] = b;
+    }
+  }
+}
+
 // Adam on the FP32 masters (Kingma & Ba, with the bias corrections applied as torch.optim.Adam
 // applies them): m = b1 m + (1-b1) g, v = b2 v + (1-b2) g^2,
 // w -= (lr / bc1) * m / (sqrt(v) / sqrt(bc2) + eps), with bc1 = 1 - b1^t and bc2 = 1 - b2^t
-// precomputed on the host as step = lr / bc1 and bc2_sqrt = sqrt(bc2).
+// precomputed on the host as step = lr / bc1 and bc2_sqrt = sqrt(bc2).  The updated weights'
+// BF16 copies are written in the same pass.
 __global__ void adam_kernel(float *w, float *m, float *v, const float *grad, long long n, float step, float bc2_sqrt,
-                            float b1, float b2, float eps) {
+                            float b1, float b2, float eps, const BfCopies copies) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float gr = grad[i];
@@ -489,17 +511,15 @@ __global__ void adam_kernel(float *w, float *m, float *v, const float *grad, lon
   const float vi = b2 * v[i] + (1.f - b2) * gr * gr;
   m[i] = mi;
   v[i] = vi;
-  w[i] -= step * (mi / (sqrtf(vi) / bc2_sqrt + eps));
+  const float wi = w[i] - step * (mi / (sqrtf(vi) / bc2_sqrt + eps));
+  w[i] = wi;
+  bf_copy(copies, i, wi);
 }
 
-// BF16 copies of a [rows][cols] FP32 master: plain (optional) and transposed (optional).
-__global__ void publish_kernel(const float *w, int rows, int cols, __nv_bfloat16 *plain, __nv_bfloat16 *trans) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= rows * cols) return;
-  const int r = i / cols, c = i % cols;
-  const __nv_bfloat16 b = __float2bfloat16_rn(w[i]);
-  if (plain) plain[i] = b;
-  if (trans) trans[c * rows + r] = b;
+// The BF16 copies of the whole parameter vector's matrices, without an update.
+__global__ void publish_kernel(const float *w, long long n, const BfCopies copies) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) bf_copy(copies, i, w[i]);
 }
 
 } // namespace bude

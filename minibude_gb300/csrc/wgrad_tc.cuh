@@ -70,7 +70,7 @@ struct WgTcArgs {
   const int *row_type;                   // [rows]
   const __nv_bfloat16 *Z1, *Z2, *Z3;     // [tiled_rows(rows)][128] pre-activations, row-tiled
   const __nv_bfloat16 *dZ1, *dZ2, *dZ3;  // [tiled_rows(rows)][128], row-tiled; zero past the end
-  const float *dy;                       // [rows]
+  const float *dy;                       // [rows] (dy and row_type allocated for tiled_rows(rows))
   int rows;
   float *part;                           // [gridDim.x][kWgPart]
   unsigned int *err;                     // bit 0: a bounded wait ran out
@@ -176,11 +176,21 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs 
     wg_load_half(a.dZ2, row, h, ad2);
     wg_load_half(a.Z1, row, h, az1);
   };
+  // The next tile's rows are prefetched into L2 while this one is staged and multiplied.
+  auto prefetch = [&](int tile) {
+    constexpr uint32_t kZ = kWgTile * kHid * 2, kX = kWgTile * kFeat * 2;
+    for (const __nv_bfloat16 *z : {a.dZ3, a.Z2, a.dZ2, a.Z1, a.dZ1, a.Z3})
+      prefetch_l2(reinterpret_cast<const unsigned char *>(z) + (long long)tile * kZ, kZ);
+    prefetch_l2(reinterpret_cast<const unsigned char *>(a.X) + (long long)tile * kX, kX);
+    prefetch_l2(a.dy + (long long)tile * kWgTile, kWgTile * 4);
+    prefetch_l2(a.row_type + (long long)tile * kWgTile, kWgTile * 4);
+  };
   if (t0 < t1) load_a(t0);
   for (int tile = t0; tile < t1; ++tile) {
     const long long row = (long long)tile * kWgTile + r;
     const bool valid = row < a.rows;
     const bool first = tile == t0;
+    if (tid == 0 && tile + 1 < t1) prefetch(tile + 1);
     // Phase A: layers 3 and 2.
     wg_store_half(R + kWgA3, kHid, h, r, ad3, false);
     wg_store_half(R + kWgB3, kWgN3, h, r, az2, true);
@@ -292,14 +302,18 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs 
 }
 
 // dEmb[t][j] = sum_f W1[f][j] S[f][t] (W1 as the forward pass used it: BF16), for the 64 x 16
-// embedding entries; S summed over blocks already.
+// embedding entries; S summed over blocks already.  One warp per entry: lane l takes f = l, l + 32,
+// ..., and the lanes' sums are folded by a fixed butterfly, so the result is the same on every run.
 __global__ void emb_grad_kernel(const float *S, const __nv_bfloat16 *w1, float *demb) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = (int)(threadIdx.x & 31);
   if (i >= kMaxTypes * kEmb) return;
   const int t = i / kEmb, j = i % kEmb;
   float acc = 0.f;
-  for (int f = 0; f < kHid; ++f) acc = fmaf(__bfloat162float(w1[f * kFeat + j]), S[f * kMaxTypes + t], acc);
-  demb[i] = acc;
+#pragma unroll
+  for (int f = lane; f < kHid; f += 32) acc = fmaf(__bfloat162float(w1[f * kFeat + j]), S[f * kMaxTypes + t], acc);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+  if (lane == 0) demb[i] = acc;
 }
 
 } // namespace bude
