@@ -68,6 +68,15 @@ __device__ __forceinline__ uint32_t act_pair(float z0, float z1) {
   return pack_bf16(h.x, h.y);
 }
 
+// The same activation of two values kept in FP32 (the output layer's input: y = w4 . h3 is
+// computed on the FMA pipe, so h3 is not rounded to BF16).
+__device__ __forceinline__ float2 act_f2(float z0, float z1) {
+  float s0, s1;
+  asm("fma.rn.sat.f32 %0, %1, %2, 0f3F000000;" : "=f"(s0) : "f"(z0), "f"(kActSlope));
+  asm("fma.rn.sat.f32 %0, %1, %2, 0f3F000000;" : "=f"(s1) : "f"(z1), "f"(kActSlope));
+  return mul2(make_float2(z0, z1), make_float2(s0, s1));
+}
+
 // dh/dz: 0 below -3, 1 above 3, z / 3 + 1/2 between.
 __device__ __forceinline__ float act_grad(float z) {
   return z <= -3.f ? 0.f : (z >= 3.f ? 1.f : fmaf(z, 2.f * kActSlope, 0.5f));

@@ -14,10 +14,10 @@
 //      signalled through the group's mbarrier;
 //   3. after each layer loads its row of D (= z) from TMEM, applies the activation (mlp.cuh:
 //      act_pair, FMA pipe only) and writes the BF16 row back into `act` as the next layer's input;
-//   4. computes the output layer on the FMA pipe from the layer-3 accumulators: h3 (rounded to
-//      BF16, the operand a fourth UMMA would read) . w4 in FP32, added to the pose's energy.  (An
-//      N = 16 UMMA for it spent a fifth of the tensor time on 1% of the FLOPs and a fourth UMMA
-//      round trip per atom; measured 251 M poses/s with it, 257 M without.)
+//   4. computes the output layer on the FMA pipe from the layer-3 accumulators: h3 (in FP32:
+//      mlp.cuh act_f2) . w4, added to the pose's energy.  (An N = 16 UMMA for it spent a fifth of
+//      the tensor time on 1% of the FLOPs and a fourth UMMA round trip per atom; measured 251 M
+//      poses/s with it, 257 M without.)
 // The bias enters as a K = 16 UMMA of a tile of ones against b_l split into three BF16 parts
 // (k = 0, 1, 2), so no FP32 add is left in the epilogue.  The groups of a block share the weights in
 // shared memory and interleave, so one group's epilogue overlaps another's MMAs.  Every mbarrier
@@ -215,8 +215,7 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
                      "r"(fp[7]), "r"(tn));
       }
       layer_wait();
-      // Output layer on the FMA pipe: h3 (rounded to BF16, as the next UMMA would read it) . w4
-      // straight from the layer-3 accumulators.
+      // Output layer on the FMA pipe: h3 (FP32) . w4 straight from the layer-3 accumulators.
       float2 acc = make_float2(0.f, 0.f);
 #pragma unroll 1
       for (int c = 0; c < kHid / 32; ++c) {
@@ -226,10 +225,9 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
 #pragma unroll
         for (int i = 0; i < 16; i += 2) {
           const float4 w = *reinterpret_cast<const float4 *>(&s.w4f[c * 32 + 2 * i]);
-          acc = fma2(unpack_bf16(act_pair(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]))),
-                     make_float2(w.x, w.y), acc);
-          acc = fma2(unpack_bf16(act_pair(__uint_as_float(v[2 * i + 2]), __uint_as_float(v[2 * i + 3]))),
-                     make_float2(w.z, w.w), acc);
+          acc = fma2(act_f2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1])), make_float2(w.x, w.y), acc);
+          acc = fma2(act_f2(__uint_as_float(v[2 * i + 2]), __uint_as_float(v[2 * i + 3])), make_float2(w.z, w.w),
+                     acc);
         }
       }
       e += acc.x + acc.y;
@@ -324,7 +322,7 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
       for (int i = 0; i < 16; ++i) {
         const float z0 = __uint_as_float(v[2 * i]), z1 = __uint_as_float(v[2 * i + 1]);
         zb[i] = pack_bf16(z0, z1);
-        hb[i] = act_pair(z0, z1);
+        if (to_act) hb[i] = act_pair(z0, z1);
       }
       {
         // Every row of the tile (rows past the end hold the bias pre-activations: finite, and
@@ -344,8 +342,9 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
 #pragma unroll
         for (int i = 0; i < 16; i += 2) {
           const float4 w = *reinterpret_cast<const float4 *>(&s.w4f[c * 32 + 2 * i]);
-          acc = fma2(unpack_bf16(hb[i]), make_float2(w.x, w.y), acc);
-          acc = fma2(unpack_bf16(hb[i + 1]), make_float2(w.z, w.w), acc);
+          acc = fma2(act_f2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1])), make_float2(w.x, w.y), acc);
+          acc = fma2(act_f2(__uint_as_float(v[2 * i + 2]), __uint_as_float(v[2 * i + 3])), make_float2(w.z, w.w),
+                     acc);
         }
       }
     }

@@ -1,6 +1,7 @@
 """Plain PyTorch FP32 reference of the surrogate MLP (test helper): the same parameter layout as
 the library (bude_surrogate_params), BF16 rounding at the points the kernels round (weights,
-embedding, activations between layers), FP32 everywhere else."""
+embedding, activations between hidden layers), FP32 everywhere else (the last hidden layer's
+activations and the output layer)."""
 import math
 
 import numpy as np
@@ -47,7 +48,7 @@ def row_outputs(torch, P, X, types):
                    torch.as_tensor(X[:, 16:], dtype=torch.float32)], dim=1)
     h1 = bf(torch, act(torch, x @ bf(torch, P["W1"]).T + P["b1"]))
     h2 = bf(torch, act(torch, h1 @ bf(torch, P["W2"]).T + P["b2"]))
-    h3 = bf(torch, act(torch, h2 @ bf(torch, P["W3"]).T + P["b3"]))
+    h3 = act(torch, h2 @ bf(torch, P["W3"]).T + P["b3"])  # FP32: the output layer runs on the FMA pipe
     return h3 @ P["w4"] + P["b4"][0]
 
 
