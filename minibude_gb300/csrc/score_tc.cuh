@@ -158,19 +158,15 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
   };
   // Activation of the group's D rows into act (K = 128 layout), then the group barrier.
   auto epilogue = [&]() {
-#pragma unroll 1
-    for (int c = 0; c < kHid / 32; ++c) {
-      uint32_t v[32];
-      tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
-      tmem_wait_ld();
-      uint32_t h[16];
+    tmem_rows128(lane_addr, [&](int c, const uint32_t (&v)[16]) {
+      uint32_t h[8];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) h[i] = act_pair(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+      for (int i = 0; i < 8; ++i) h[i] = act_pair(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
-        *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c * 32 + q * 8, kHid)) =
+      for (int q = 0; q < 2; ++q)
+        *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c * 16 + q * 8, kHid)) =
             make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
-    }
+    });
     fence_proxy_async();
     tc_fence_before();
     named_sync(bar_id, kTcGroupThreads);
@@ -217,19 +213,15 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
       layer_wait();
       // Output layer on the FMA pipe: h3 (FP32) . w4 straight from the layer-3 accumulators.
       float2 acc = make_float2(0.f, 0.f);
-#pragma unroll 1
-      for (int c = 0; c < kHid / 32; ++c) {
-        uint32_t v[32];
-        tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
-        tmem_wait_ld();
+      tmem_rows128(lane_addr, [&](int c, const uint32_t (&v)[16]) {
 #pragma unroll
-        for (int i = 0; i < 16; i += 2) {
-          const float4 w = *reinterpret_cast<const float4 *>(&s.w4f[c * 32 + 2 * i]);
+        for (int i = 0; i < 8; i += 2) {
+          const float4 w = *reinterpret_cast<const float4 *>(&s.w4f[c * 16 + 2 * i]);
           acc = fma2(act_f2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1])), make_float2(w.x, w.y), acc);
           acc = fma2(act_f2(__uint_as_float(v[2 * i + 2]), __uint_as_float(v[2 * i + 3])), make_float2(w.z, w.w),
                      acc);
         }
-      }
+      });
       e += acc.x + acc.y;
       tc_fence_before(); // the next atom's barrier orders these TMEM reads before the next UMMA
     }

@@ -107,6 +107,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
       : "memory");
 }
 
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+}
+
 // Store 8 / 16 / 32 consecutive 32-bit columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8]) {
   asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(v[0]),
@@ -121,6 +131,26 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16
                : "memory");
 }
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// body(c, v) over the 8 chunks of 16 columns starting at taddr (c = 0..7, v = the chunk's 16 FP32
+// values), with the load of chunk c + 1 in flight while chunk c is processed: one TMEM load
+// latency per 128 columns instead of one per chunk.
+template <class F> __device__ __forceinline__ void tmem_rows128(uint32_t taddr, F &&body) {
+  uint32_t a[16], b[16];
+  tmem_ld16(taddr, a);
+  tmem_wait_ld();
+#pragma unroll
+  for (int c = 0; c < 8; c += 2) {
+    tmem_ld16(taddr + (uint32_t)((c + 1) * 16), b);
+    body(c, a);
+    tmem_wait_ld();
+    if (c + 2 < 8) tmem_ld16(taddr + (uint32_t)((c + 2) * 16), a);
+    body(c + 1, b);
+    if (c + 2 < 8) tmem_wait_ld();
+  }
+}
 
 // 2 consecutive FP32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld2(uint32_t taddr, uint32_t (&v)[2]) {
@@ -143,6 +173,5 @@ __device__ __forceinline__ bool named_sync_or(uint32_t id, uint32_t nthreads, bo
   return r != 0;
 }
 
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 } // namespace bude
