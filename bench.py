@@ -566,7 +566,7 @@ def run_surrogate(args, dist: Dist):
     out = {"metric": "surrogate poses/s", "value": round(dist.world * held.total_poses / (step * 1e-3), 1),
            "unit": "poses/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": round(step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "bf16 (fp32 accumulate)", "data": "synthetic ligands/poses (seeded) against the 938-atom protein",
+           "dtype": "fp16 scoring, bf16 training (fp32 accumulate)", "data": "synthetic ligands/poses (seeded) against the 938-atom protein",
            "config": {"workload": "surrogate-train-512x4096-held-64x65536", "train_poses": train.total_poses,
                       "held_poses": held.total_poses, "epochs": args.epochs, "batch": 8192,
                       "grid_spacing_A": args.grid_spacing,
@@ -582,8 +582,9 @@ def run_surrogate(args, dist: Dist):
                                          "+ 13 protein-field channels sampled from a trilinear grid (in place of "
                                          "nearest-protein-tile distances) = 32 features; 3 hidden layers of 128 "
                                          "with hard-swish (the piecewise-polynomial SiLU: no MUFU on the "
-                                         "critical path); BF16 weights, FP32 accumulation and Adam state; "
-                                         "summed per pose",
+                                         "critical path); trained in BF16 with FP32 accumulation and Adam "
+                                         "state, scored in FP16 (weights, features, hidden activations) with "
+                                         "FP32 accumulation and output layer; summed per pose",
                       "mma_sync_scorer_poses_per_s": round(held.total_poses / (ms_sync * 1e-3), 1),
                       "max_abs_diff_vs_mma_sync": round(float(np.max(np.abs(sur - sur_sync))), 4)},
            "gpu_launches": launches, "roofline": roof}
@@ -654,7 +655,7 @@ def run_screen(args, dist: Dist):
     out = {"metric": "screened poses/s", "value": round(dist.world * screen.total_poses / (step * 1e-3), 1),
            "unit": "poses/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": round(step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "bf16 surrogate + f32 exact",
+           "dtype": "fp16 surrogate + f32 exact",
            "data": "synthetic ligands/poses (seeded) against the reference's bm2 protein",
            "config": {"workload": "screen-1024x16384", "poses": screen.total_poses, "top_frac": 0.02,
                       "audit_frac": 0.005, "audit_tol": 0.05, "epochs": args.epochs, "train_ms": round(train_ms, 1),
@@ -681,7 +682,8 @@ def run_screen(args, dist: Dist):
                                          "+ 13 protein-field channels sampled from a trilinear grid (in place of "
                                          "nearest-protein-tile distances) = 32 features; 3 hidden layers of 128 "
                                          "with hard-swish (the piecewise-polynomial SiLU: no MUFU on the "
-                                         "critical path); BF16 weights, FP32 accumulation; summed per pose",
+                                         "critical path); scored in FP16 (weights, features, hidden "
+                                         "activations) with FP32 accumulation and output layer; summed per pose",
                       "exact_launch": cfg.as_dict(), "screen_exact_launch": scfg.as_dict()},
            "gpu_launches": launches, "clocks": clk}
     # dominant kernel: the surrogate scorer over every pose

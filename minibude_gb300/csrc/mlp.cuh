@@ -77,6 +77,24 @@ __device__ __forceinline__ float2 act_f2(float z0, float z1) {
   return mul2(make_float2(z0, z1), make_float2(s0, s1));
 }
 
+// FP16 pair (lo in the low half), rounded to nearest and saturated to the largest finite value.
+__device__ __forceinline__ uint32_t pack_f16(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+
+// The activation for the FP16 scorer: z rounded to FP16, then s = sat(z / 6 + 1/2) and z * s as
+// packed FP16 instructions (three instructions per pair; FP16 keeps 11 significant bits, so the
+// result is closer to the FP32 activation than the BF16-rounded one the training pass uses).
+__device__ __forceinline__ uint32_t act_pair_f16(float z0, float z1) {
+  const uint32_t zh = pack_f16(z0, z1);
+  uint32_t s, h;
+  asm("fma.rn.sat.f16x2 %0, %1, %2, %3;" : "=r"(s) : "r"(zh), "r"(0x31553155u), "r"(0x38003800u)); // 1/6, 1/2
+  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(h) : "r"(zh), "r"(s));
+  return h;
+}
+
 // dh/dz: 0 below -3, 1 above 3, z / 3 + 1/2 between.
 __device__ __forceinline__ float act_grad(float z) {
   return z <= -3.f ? 0.f : (z >= 3.f ? 1.f : fmaf(z, 2.f * kActSlope, 0.5f));

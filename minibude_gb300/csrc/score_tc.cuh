@@ -1,5 +1,11 @@
 // score_tc.cuh -- surrogate inference on the 5th-generation tensor cores (tcgen05 + TMEM).
 //
+// The scorer computes in FP16 (weights, features and activations; FP32 accumulators and output
+// layer): FP16's packed FMA has the saturation the activation needs (mlp.cuh act_pair_f16), one
+// instruction per pair fewer than BF16 on the epilogue's critical path, and its 11 significant bits
+// put the scores closer to the FP32 network than the BF16 training pass.  The training forward
+// pass below runs the same chain in BF16.
+//
 // A block runs G independent tile groups of 128 threads (G = 4 for scoring alone; G = 3 leaves
 // shared memory and registers on each SM for exact-kernel blocks, which the screening pipeline
 // runs beside it).  A group scores one item at a
@@ -12,13 +18,14 @@
 //   2. runs layers 1..3 as UMMAs issued by the group's first thread: D[128 x 128] = 1 * B_l^T
 //      (the bias) + act * W_l^T over K = 32, 128, 128, FP32 accumulators in TMEM, completion
 //      signalled through the group's mbarrier;
-//   3. after each layer loads its row of D (= z) from TMEM, applies the activation (mlp.cuh:
-//      act_pair, FMA pipe only) and writes the BF16 row back into `act` as the next layer's input;
+//   3. after each layer loads its row of D (= z) from TMEM (tc.cuh tmem_rows128: 16 columns at a
+//      time, the next chunk's load in flight), applies the activation (mlp.cuh: act_pair_f16)
+//      and writes the FP16 row back into `act` as the next layer's input;
 //   4. computes the output layer on the FMA pipe from the layer-3 accumulators: h3 (in FP32:
 //      mlp.cuh act_f2) . w4, added to the pose's energy.  (An N = 16 UMMA for it spent a fifth of
 //      the tensor time on 1% of the FLOPs and a fourth UMMA round trip per atom; measured 251 M
 //      poses/s with it, 257 M without.)
-// The bias enters as a K = 16 UMMA of a tile of ones against b_l split into three BF16 parts
+// The bias enters as a K = 16 UMMA of a tile of ones against b_l split into three 16-bit parts
 // (k = 0, 1, 2), so no FP32 add is left in the epilogue.  The groups of a block share the weights in
 // shared memory and interleave, so one group's epilogue overlaps another's MMAs.  Every mbarrier
 // wait is bounded; a wait that runs out sets bit 0 of the error word, the group leaves at its next
@@ -40,11 +47,11 @@ template <int G> struct TcSmem {
   alignas(128) unsigned char w1[kHid * kFeat * 2];          // W1: [128 out][32 in], K-major
   alignas(128) unsigned char w2[kHid * kHid * 2];           // W2
   alignas(128) unsigned char w3[kHid * kHid * 2];           // W3
-  alignas(128) unsigned char bias[3][kHid * kTcBiasK * 2];  // b_l in three BF16 parts at k = 0..2
+  alignas(128) unsigned char bias[3][kHid * kTcBiasK * 2];  // b_l in three 16-bit parts at k = 0..2
   alignas(128) unsigned char ones[kHid * kTcBiasK * 2];     // 1 at k = 0..2
   alignas(128) unsigned char act[G][kHid * kHid * 2];         // per group: the layer input tile
   alignas(16) float w4f[kHid];                               // output weights, FP32
-  uint4 emb[kMaxTypes * 2];                                  // type embeddings (16 BF16 each)
+  uint4 emb[kMaxTypes * 2];                                  // type embeddings (16 x 16 bits each)
   alignas(8) uint64_t bar[G];
   int item[G]; // per group: the tile it took from a work counter (training forward pass)
   uint32_t tmem;
@@ -60,26 +67,42 @@ static_assert(sizeof(TcSmem<3>) > 114 * 1024, "shared memory keeps a second scor
 // TMEM columns a block allocates: a power of two covering G groups of 128.
 template <int G> __host__ __device__ constexpr int tc_alloc_cols() { return G * kTcCols <= 256 ? 256 : 512; }
 
+// The weights a tcgen05 kernel stages: 16-bit matrices ([out][in]; BF16, or FP16 for the scorer)
+// and the FP32 vectors.
+struct TcWeights {
+  const void *emb, *w1, *w2, *w3;
+  const float *b1, *b2, *b3, *w4, *b4;
+};
+__host__ __device__ inline TcWeights tc_weights(const MlpWeights &W) {
+  return TcWeights{W.emb, W.w1, W.w2, W.w3, W.b1, W.b2, W.b3, W.w4, W.b4};
+}
+
 struct ScoreTcArgs {
-  ScoreArgs s;
+  ScoreArgs s;   // s.W unused: the scorer reads the FP16 copies in w
+  TcWeights w;   // FP16 matrices and embeddings
   unsigned int *err;
 };
 
-__device__ __forceinline__ void st_bf16(unsigned char *tile, uint32_t off, float v) {
-  *reinterpret_cast<__nv_bfloat16 *>(tile + off) = __float2bfloat16_rn(v);
+template <bool F16> __device__ __forceinline__ void st_16(unsigned char *tile, uint32_t off, float v) {
+  if (F16) *reinterpret_cast<__half *>(tile + off) = __float2half_rn(v);
+  else *reinterpret_cast<__nv_bfloat16 *>(tile + off) = __float2bfloat16_rn(v);
+}
+template <bool F16> __device__ __forceinline__ float round_16(float v) {
+  return F16 ? __half2float(__float2half_rn(v)) : __bfloat162float(__float2bfloat16_rn(v));
 }
 
-// Copy a global [N][K] row-major BF16 matrix into the K-major core-matrix layout.
-__device__ __forceinline__ void to_kmajor(unsigned char *dst, const __nv_bfloat16 *src, int n, int k) {
+// Copy a global [N][K] row-major 16-bit matrix into the K-major core-matrix layout.
+__device__ __forceinline__ void to_kmajor(unsigned char *dst, const void *src, int n, int k) {
+  const uint4 *s16 = reinterpret_cast<const uint4 *>(src);
   for (int i = threadIdx.x; i < n * k / 8; i += blockDim.x) {
     const int row = i / (k / 8), k8 = i % (k / 8);
-    *reinterpret_cast<uint4 *>(dst + kmajor_offset(row, k8 * 8, k)) =
-        __ldg(reinterpret_cast<const uint4 *>(src + (long long)row * k + k8 * 8));
+    *reinterpret_cast<uint4 *>(dst + kmajor_offset(row, k8 * 8, k)) = __ldg(s16 + (long long)row * (k / 8) + k8);
   }
 }
 
-// The block's constant tiles: weights, bias tiles, the ones tile, output weights, embeddings.
-template <class Smem> __device__ __forceinline__ void tc_setup(Smem &s, const MlpWeights &W) {
+// The block's constant tiles: weights, bias tiles, the ones tile, output weights, embeddings, in
+// BF16 or (F16) FP16.
+template <bool F16, class Smem> __device__ __forceinline__ void tc_setup(Smem &s, const TcWeights &W) {
   const int tid = threadIdx.x;
   {
     uint4 *z = reinterpret_cast<uint4 *>(s.bias);
@@ -96,14 +119,14 @@ template <class Smem> __device__ __forceinline__ void tc_setup(Smem &s, const Ml
     const int l = i / kHid, n = i % kHid;
     const float *b = l == 0 ? W.b1 : (l == 1 ? W.b2 : W.b3);
     const float v = __ldg(&b[n]);
-    const float hi = __bfloat162float(__float2bfloat16_rn(v));
-    const float mid = __bfloat162float(__float2bfloat16_rn(v - hi));
-    st_bf16(s.bias[l], kmajor_offset(n, 0, kTcBiasK), hi);
-    st_bf16(s.bias[l], kmajor_offset(n, 1, kTcBiasK), mid);
-    st_bf16(s.bias[l], kmajor_offset(n, 2, kTcBiasK), v - hi - mid);
+    const float hi = round_16<F16>(v);
+    const float mid = round_16<F16>(v - hi);
+    st_16<F16>(s.bias[l], kmajor_offset(n, 0, kTcBiasK), hi);
+    st_16<F16>(s.bias[l], kmajor_offset(n, 1, kTcBiasK), mid);
+    st_16<F16>(s.bias[l], kmajor_offset(n, 2, kTcBiasK), v - hi - mid);
   }
   for (int m = tid; m < kHid; m += blockDim.x)
-    for (int k = 0; k < 3; ++k) st_bf16(s.ones, kmajor_offset(m, k, kTcBiasK), 1.f);
+    for (int k = 0; k < 3; ++k) st_16<F16>(s.ones, kmajor_offset(m, k, kTcBiasK), 1.f);
 }
 
 template <int G>
@@ -114,7 +137,7 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
   const int tid = threadIdx.x, g = tid / kTcGroupThreads, lt = tid % kTcGroupThreads;
   const uint32_t bar_id = 1 + g; // named barrier of the group
 
-  tc_setup(s, a.W);
+  tc_setup<true>(s, A.w);
   if (tid == 0) {
     for (int q = 0; q < G; ++q) mbar_init(&s.bar[q], 1);
     mbar_fence_init();
@@ -129,8 +152,8 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
   const uint32_t lane_addr = tmem + ((uint32_t)((lt / 32) * 32) << 16);
   unsigned char *act = s.act[g];
   const uint32_t act_a = smem_u32(act), ones_a = smem_u32(s.ones);
-  const uint32_t idesc = umma_idesc_bf16(kHid, kHid);
-  const float b4 = __ldg(a.W.b4);
+  const uint32_t idesc = umma_idesc_f16(kHid, kHid);
+  const float b4 = __ldg(A.w.b4);
   uint64_t *bar = &s.bar[g];
   uint32_t phase = 0;
   bool failed = false;
@@ -161,7 +184,7 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
     tmem_rows128(lane_addr, [&](int c, const uint32_t (&v)[16]) {
       uint32_t h[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) h[i] = act_pair(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+      for (int i = 0; i < 8; ++i) h[i] = act_pair_f16(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
 #pragma unroll
       for (int q = 0; q < 2; ++q)
         *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c * 16 + q * 8, kHid)) =
@@ -185,7 +208,7 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
     auto fetch = [&](int il) {
       const float4 la = __ldg(&a.ligands[it.x + il]);
       tn = __float_as_int(la.w);
-      field_features(a.g, la, r0, r1, r2, fp);
+      field_features<true>(a.g, la, r0, r1, r2, fp);
     };
     if (it.y > 0) fetch(0);
     for (int il = 0; il < it.y; ++il) {
@@ -266,7 +289,7 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
   const int tid = threadIdx.x, g = tid / kTcGroupThreads, lt = tid % kTcGroupThreads;
   const uint32_t bar_id = 1 + g;
 
-  tc_setup(s, A.W);
+  tc_setup<false>(s, tc_weights(A.W));
   if (tid == 0) {
     for (int q = 0; q < G; ++q) mbar_init(&s.bar[q], 1);
     mbar_fence_init();
@@ -304,42 +327,36 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
   // or, after layer 3, w4 . act(z) -> y.
   auto epilogue = [&](__nv_bfloat16 *Z, long long row, bool valid, bool to_act, float *yout) {
     float2 acc = make_float2(0.f, 0.f);
-#pragma unroll 1
-    for (int c = 0; c < kHid / 32; ++c) {
-      uint32_t v[32];
-      tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
-      tmem_wait_ld();
-      uint32_t zb[16], hb[16];
+    // Every row of the tile is stored (rows past the end hold the bias pre-activations: finite,
+    // and their gradients are zero), so each warp store fills whole 128-byte lines.
+    unsigned char *zt = reinterpret_cast<unsigned char *>(Z) + tiled_offset(row, 0, kHid);
+    tmem_rows128(lane_addr, [&](int c, const uint32_t (&v)[16]) {
+      uint32_t zb[8], hb[8];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
+      for (int i = 0; i < 8; ++i) {
         const float z0 = __uint_as_float(v[2 * i]), z1 = __uint_as_float(v[2 * i + 1]);
         zb[i] = pack_bf16(z0, z1);
         if (to_act) hb[i] = act_pair(z0, z1);
       }
-      {
-        // Every row of the tile (rows past the end hold the bias pre-activations: finite, and
-        // their gradients are zero), so each warp store fills whole 128-byte lines.
-        unsigned char *zt = reinterpret_cast<unsigned char *>(Z) + tiled_offset(row, 0, kHid);
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-          *reinterpret_cast<uint4 *>(zt + kmajor_offset(0, c * 32 + q * 8, kHid)) =
-              make_uint4(zb[4 * q], zb[4 * q + 1], zb[4 * q + 2], zb[4 * q + 3]);
-      }
+      for (int q = 0; q < 2; ++q)
+        *reinterpret_cast<uint4 *>(zt + kmajor_offset(0, c * 16 + q * 8, kHid)) =
+            make_uint4(zb[4 * q], zb[4 * q + 1], zb[4 * q + 2], zb[4 * q + 3]);
       if (to_act) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-          *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c * 32 + q * 8, kHid)) =
+        for (int q = 0; q < 2; ++q)
+          *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c * 16 + q * 8, kHid)) =
               make_uint4(hb[4 * q], hb[4 * q + 1], hb[4 * q + 2], hb[4 * q + 3]);
       } else {
 #pragma unroll
-        for (int i = 0; i < 16; i += 2) {
-          const float4 w = *reinterpret_cast<const float4 *>(&s.w4f[c * 32 + 2 * i]);
+        for (int i = 0; i < 8; i += 2) {
+          const float4 w = *reinterpret_cast<const float4 *>(&s.w4f[c * 16 + 2 * i]);
           acc = fma2(act_f2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1])), make_float2(w.x, w.y), acc);
           acc = fma2(act_f2(__uint_as_float(v[2 * i + 2]), __uint_as_float(v[2 * i + 3])), make_float2(w.z, w.w),
                      acc);
         }
       }
-    }
+    });
     if (yout && valid) *yout = acc.x + acc.y;
     if (to_act) fence_proxy_async();
     tc_fence_before();
@@ -496,22 +513,31 @@ __global__ void __launch_bounds__(kBwdGroups * kTcGroupThreads, 1) train_backwar
             make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
     }
   };
+  auto put16 = [&](__nv_bfloat16 *dZ, long long row, int c0, const uint32_t (&d)[8], bool to_act) {
+    unsigned char *dt = reinterpret_cast<unsigned char *>(dZ) + tiled_offset(row, 0, kHid);
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+      *reinterpret_cast<uint4 *>(dt + kmajor_offset(0, c0 + q * 8, kHid)) =
+          make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
+    if (to_act) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        *reinterpret_cast<uint4 *>(act + kmajor_offset(lt, c0 + q * 8, kHid)) =
+            make_uint4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
+    }
+  };
   // dz = D (from TMEM) * act'(z) for the row's pre-activations z (in registers).
   auto through = [&](const uint4 (&z)[16], __nv_bfloat16 *dZ, long long row, bool to_act) {
+    tmem_rows128(lane_addr, [&](int c, const uint32_t (&v)[16]) {
+      const uint32_t *zw = reinterpret_cast<const uint32_t *>(&z[2 * c]);
+      uint32_t d[8];
 #pragma unroll
-    for (int c = 0; c < kHid / 32; ++c) {
-      uint32_t v[32];
-      tmem_ld32(lane_addr + (uint32_t)(c * 32), v);
-      tmem_wait_ld();
-      const uint32_t *zw = reinterpret_cast<const uint32_t *>(&z[4 * c]);
-      uint32_t d[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
+      for (int i = 0; i < 8; ++i) {
         const float2 zz = unpack_bf16(zw[i]);
         d[i] = pack_bf16(__uint_as_float(v[2 * i]) * act_grad(zz.x), __uint_as_float(v[2 * i + 1]) * act_grad(zz.y));
       }
-      put(dZ, row, c * 32, d, to_act);
-    }
+      put16(dZ, row, c * 16, d, to_act);
+    });
   };
 
   for (;;) {

@@ -43,6 +43,7 @@ struct Surrogate {
   int ntypes = 0;
   DevBuf params, adam_m, adam_v, grads;
   DevBuf emb_bf, w1_bf, w2_bf, w3_bf, w1t_bf, w2t_bf, w3t_bf;
+  DevBuf emb_h, w1_h, w2_h, w3_h; // FP16 copies for the tcgen05 scorer
   DevBuf grid, protein4;
   cudaArray_t tex_arr[4] = {};
   cudaTextureObject_t tex[4] = {};
@@ -79,7 +80,7 @@ void release_surrogate(Context &c) {
   Surrogate &s = *c.surrogate;
   release_textures(s);
   DevBuf *all[] = {&s.params, &s.adam_m, &s.adam_v, &s.grads, &s.emb_bf, &s.w1_bf, &s.w2_bf, &s.w3_bf,
-                   &s.w1t_bf, &s.w2t_bf, &s.w3t_bf, &s.grid, &s.protein4, &s.X, &s.row_type, &s.Z1,
+                   &s.w1t_bf, &s.w2t_bf, &s.w3t_bf, &s.emb_h, &s.w1_h, &s.w2_h, &s.w3_h, &s.grid, &s.protein4, &s.X, &s.row_type, &s.Z1,
                    &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3, &s.y, &s.dy, &s.pred, &s.loss, &s.dsum,
                    &s.part_w, &s.S_sum, &s.labels, &s.pose_lig_first, &s.pose_lig_n,
                    &s.epoch_pose, &s.epoch_rowoff, &s.items, &s.scores, &s.next};
@@ -106,18 +107,19 @@ static MlpWeights weights(Surrogate &s) {
 // The BF16 copies of the weights (plain, and transposed for the backward pass).
 static BfCopies bf_copies(Surrogate &s) {
   BfCopies c{};
-  auto add = [&](long long off, int rows, int cols, DevBuf *plain, DevBuf *trans) {
+  auto add = [&](long long off, int rows, int cols, DevBuf *plain, DevBuf *trans, DevBuf *half) {
     const int k = c.n++;
     c.off[k] = off;
     c.rows[k] = rows;
     c.cols[k] = cols;
     c.plain[k] = plain ? plain->as<__nv_bfloat16>() : nullptr;
     c.trans[k] = trans ? trans->as<__nv_bfloat16>() : nullptr;
+    c.half[k] = half ? half->as<__half>() : nullptr;
   };
-  add(kOffEmb, kMaxTypes, kEmb, &s.emb_bf, nullptr);
-  add(kOffW1, kHid, kFeat, &s.w1_bf, &s.w1t_bf);
-  add(kOffW2, kHid, kHid, &s.w2_bf, &s.w2t_bf);
-  add(kOffW3, kHid, kHid, &s.w3_bf, &s.w3t_bf);
+  add(kOffEmb, kMaxTypes, kEmb, &s.emb_bf, nullptr, &s.emb_h);
+  add(kOffW1, kHid, kFeat, &s.w1_bf, &s.w1t_bf, &s.w1_h);
+  add(kOffW2, kHid, kHid, &s.w2_bf, &s.w2t_bf, &s.w2_h);
+  add(kOffW3, kHid, kHid, &s.w3_bf, &s.w3t_bf, &s.w3_h);
   return c;
 }
 
@@ -239,6 +241,10 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
   if (!rc) rc = s.w2t_bf.reserve(kHid * kHid * 2, "w2t bf16");
   if (!rc) rc = s.w3_bf.reserve(kHid * kHid * 2, "w3 bf16");
   if (!rc) rc = s.w3t_bf.reserve(kHid * kHid * 2, "w3t bf16");
+  if (!rc) rc = s.emb_h.reserve(kMaxTypes * kEmb * 2, "emb fp16");
+  if (!rc) rc = s.w1_h.reserve(kHid * kFeat * 2, "w1 fp16");
+  if (!rc) rc = s.w2_h.reserve(kHid * kHid * 2, "w2 fp16");
+  if (!rc) rc = s.w3_h.reserve(kHid * kHid * 2, "w3 fp16");
   if (rc) return rc;
   cudaError_t e = copy_sync(c, s.params.ptr, p.data(), pb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = fill_sync(c, s.adam_m.ptr, 0, pb);
@@ -742,6 +748,7 @@ int surrogate_score_range(Context &c, int lig0, int lig1, int groups, cudaStream
   if (s.scorer == BUDE_SCORER_TCGEN05) {
     ScoreTcArgs t;
     t.s = a;
+    t.w = TcWeights{s.emb_h.ptr, s.w1_h.ptr, s.w2_h.ptr, s.w3_h.ptr, a.W.b1, a.W.b2, a.W.b3, a.W.w4, a.W.b4};
     t.err = c.err.as<unsigned int>();
     // One block per SM: a block holds all of its SM's TMEM it allocates.
     const int g = groups == 3 ? 3 : 4;

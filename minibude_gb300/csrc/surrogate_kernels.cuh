@@ -153,8 +153,9 @@ __device__ __forceinline__ void sample_field(const FieldGrid &g, float x, float 
 }
 
 // Features 16..31 of one (pose, ligand atom) -- the transformed position x 0.1 and the 13 field
-// channels -- as 8 packed BF16 pairs, from the atom {x, y, z, type bits} and the pose's transform
-// rows r0..r2 ({R row, t}).
+// channels -- as 8 packed BF16 pairs (FP16 pairs when F16), from the atom {x, y, z, type bits} and
+// the pose's transform rows r0..r2 ({R row, t}).
+template <bool F16 = false>
 __device__ __forceinline__ void field_features(const FieldGrid &g, float4 la, float4 r0, float4 r1, float4 r2,
                                                uint32_t (&p)[8]) {
   const float x = r0.w + la.x * r0.x + la.y * r0.y + la.z * r0.z;
@@ -162,14 +163,15 @@ __device__ __forceinline__ void field_features(const FieldGrid &g, float4 la, fl
   const float z = r2.w + la.x * r2.x + la.y * r2.y + la.z * r2.z;
   float c[kGridCh];
   sample_field(g, x, y, z, c);
-  p[0] = pack_bf16(x * g.xyz_scale, y * g.xyz_scale);
-  p[1] = pack_bf16(z * g.xyz_scale, c[0]);
-  p[2] = pack_bf16(c[1], c[2]);
-  p[3] = pack_bf16(c[3], c[4]);
-  p[4] = pack_bf16(c[5], c[6]);
-  p[5] = pack_bf16(c[7], c[8]);
-  p[6] = pack_bf16(c[9], c[10]);
-  p[7] = pack_bf16(c[11], c[12]);
+  auto pk = [](float lo, float hi) { return F16 ? pack_f16(lo, hi) : pack_bf16(lo, hi); };
+  p[0] = pk(x * g.xyz_scale, y * g.xyz_scale);
+  p[1] = pk(z * g.xyz_scale, c[0]);
+  p[2] = pk(c[1], c[2]);
+  p[3] = pk(c[3], c[4]);
+  p[4] = pk(c[5], c[6]);
+  p[5] = pk(c[7], c[8]);
+  p[6] = pk(c[9], c[10]);
+  p[7] = pk(c[11], c[12]);
 }
 
 // Features of one (pose, ligand atom) as 16 packed BF16 pairs: the type's embedding e0, e1
@@ -475,12 +477,14 @@ __global__ void __launch_bounds__(32 * kReduceWarps) reduce_segments_kernel(cons
   }
 }
 
-// BF16 copies of FP32 master matrices inside the parameter vector: matrix k is the [rows][cols]
-// block at off[k], copied plainly and/or transposed (null pointers skip a copy).
+// 16-bit copies of FP32 master matrices inside the parameter vector: matrix k is the [rows][cols]
+// block at off[k], copied to BF16 plainly and/or transposed, and to FP16 plainly (null pointers
+// skip a copy).
 struct BfCopies {
   long long off[4];
   int rows[4], cols[4];
   __nv_bfloat16 *plain[4], *trans[4];
+  __half *half[4];
   int n;
 };
 
@@ -493,6 +497,7 @@ __device__ __forceinline__ void bf_copy(const BfCopies &c, long long i, float w)
       const __nv_bfloat16 b = __float2bfloat16_rn(w);
       if (c.plain[k]) c.plain[k][j] = b;
       if (c.trans[k]) c.trans[k][(long long)col * c.rows[k] + r] = b;
+      if (c.half[k]) c.half[k][j] = __float2half_rn(w);
     }
   }
 }

@@ -48,6 +48,11 @@ __host__ __device__ constexpr uint32_t umma_idesc_bf16(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
+// The same with A and B FP16 (bits 7-12 = 0).
+__host__ __device__ constexpr uint32_t umma_idesc_f16(int m, int n) {
+  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
 // Allocate `ncols` TMEM columns (power of two >= 32) for this CTA; executed by one whole warp.
 // The TMEM address is written to the shared-memory word `slot`.
 template <int NCOLS> __device__ __forceinline__ void tmem_alloc(uint32_t *slot) {

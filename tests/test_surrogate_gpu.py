@@ -50,8 +50,10 @@ def test_forward_matches_torch(setup):
 
 
 def test_tcgen05_and_mma_sync_scorers_agree(setup):
-    """The tensor-memory scorer and the warp-level one evaluate the same network; only their FP32
-    summation order differs, which may move a hidden activation by one BF16 step."""
+    """The tensor-memory scorer and the warp-level one evaluate the same network, the first in FP16
+    (weights, features, activations) and the second in BF16 as the training pass does.  Rounding
+    an activation to BF16 moves it by up to 2^-9 of its value, and through the convex hard-swish
+    that noise raises the BF16 chain's energies by a few tenths of a per cent on average."""
     ctx, batch = setup
     out = {}
     for kind in ("mma_sync", "tcgen05"):
@@ -60,7 +62,7 @@ def test_tcgen05_and_mma_sync_scorers_agree(setup):
         out[kind] = ctx.surrogate_download()
     scale = np.maximum(np.abs(out["mma_sync"]), 1.0)
     assert np.all(np.isfinite(out["tcgen05"]))
-    assert np.max(np.abs(out["tcgen05"] - out["mma_sync"]) / scale) < 5e-3
+    assert np.max(np.abs(out["tcgen05"] - out["mma_sync"]) / scale) < 1e-2
     with pytest.raises(ValueError):
         ctx.surrogate_set_scorer("wmma")
 
