@@ -81,6 +81,8 @@ struct ScoreTcArgs {
   ScoreArgs s;   // s.W unused: the scorer reads the FP16 copies in w
   TcWeights w;   // FP16 matrices and embeddings
   unsigned int *err;
+  float w4[kHid]; // output weights as launch parameters: operands of the output layer's FMAs
+                  // straight from the constant bank, no shared-memory loads
 };
 
 template <bool F16> __device__ __forceinline__ void st_16(unsigned char *tile, uint32_t off, float v) {
@@ -234,16 +236,14 @@ __global__ void __launch_bounds__(G * kTcGroupThreads, 1) score_tc_kernel(const 
                      "r"(fp[7]), "r"(tn));
       }
       layer_wait();
-      // Output layer on the FMA pipe: h3 (FP32) . w4 straight from the layer-3 accumulators.
+      // Output layer on the FMA pipe: h3 (FP32) . w4 straight from the layer-3 accumulators (two
+      // FP32 partial sums, even and odd features).
       float2 acc = make_float2(0.f, 0.f);
       tmem_rows128(lane_addr, [&](int c, const uint32_t (&v)[16]) {
 #pragma unroll
-        for (int i = 0; i < 8; i += 2) {
-          const float4 w = *reinterpret_cast<const float4 *>(&s.w4f[c * 16 + 2 * i]);
-          acc = fma2(act_f2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1])), make_float2(w.x, w.y), acc);
-          acc = fma2(act_f2(__uint_as_float(v[2 * i + 2]), __uint_as_float(v[2 * i + 3])), make_float2(w.z, w.w),
-                     acc);
-        }
+        for (int i = 0; i < 8; ++i)
+          acc = fma2(act_f2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1])),
+                     make_float2(A.w4[c * 16 + 2 * i], A.w4[c * 16 + 2 * i + 1]), acc);
       });
       e += acc.x + acc.y;
       tc_fence_before(); // the next atom's barrier orders these TMEM reads before the next UMMA

@@ -44,6 +44,8 @@ struct Surrogate {
   DevBuf params, adam_m, adam_v, grads;
   DevBuf emb_bf, w1_bf, w2_bf, w3_bf, w1t_bf, w2t_bf, w3t_bf;
   DevBuf emb_h, w1_h, w2_h, w3_h; // FP16 copies for the tcgen05 scorer
+  float w4_host[kHid] = {};        // host copy of the output weights (scorer launch parameters)
+  bool w4_host_valid = false;      // false whenever the weights may have changed
   DevBuf grid, protein4;
   cudaArray_t tex_arr[4] = {};
   cudaTextureObject_t tex[4] = {};
@@ -125,6 +127,7 @@ static BfCopies bf_copies(Surrogate &s) {
 
 // Refresh the BF16 copies of the weights from the FP32 masters.
 static int publish(Context &c, Surrogate &s) {
+  s.w4_host_valid = false;
   publish_kernel<<<(unsigned)((kOffW3 + kHid * kHid + 255) / 256), 256, 0, c.stream>>>(s.params.as<float>(),
                                                                                       kOffW3 + kHid * kHid, bf_copies(s));
   cudaError_t e = cudaGetLastError();
@@ -453,6 +456,7 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
                                                                        s.w1_bf.as<__nv_bfloat16>(), gr + kOffEmb);
   if (lr > 0.f) {
     s.step++;
+    s.w4_host_valid = false;
     const float b1 = 0.9f, b2 = 0.999f;
     const double bc1 = 1.0 - std::pow((double)b1, (double)s.step), bc2 = 1.0 - std::pow((double)b2, (double)s.step);
     adam_kernel<<<(unsigned)((kNParams + 255) / 256), 256, 0, c.stream>>>(
@@ -746,8 +750,15 @@ int surrogate_score_range(Context &c, int lig0, int lig1, int groups, cudaStream
   int per_sm = 0;
   cudaError_t e;
   if (s.scorer == BUDE_SCORER_TCGEN05) {
+    if (!s.w4_host_valid) {
+      // The weights changed since the last launch (they change on the context's stream).
+      e = copy_sync(c, s.w4_host, a.W.w4, sizeof s.w4_host, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_error(e, "output weights");
+      s.w4_host_valid = true;
+    }
     ScoreTcArgs t;
     t.s = a;
+    std::memcpy(t.w4, s.w4_host, sizeof t.w4);
     t.w = TcWeights{s.emb_h.ptr, s.w1_h.ptr, s.w2_h.ptr, s.w3_h.ptr, a.W.b1, a.W.b2, a.W.b3, a.W.w4, a.W.b4};
     t.err = c.err.as<unsigned int>();
     // One block per SM: a block holds all of its SM's TMEM it allocates.
