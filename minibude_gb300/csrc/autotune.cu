@@ -30,7 +30,8 @@ static int ppwi_to_p(int ppwi) {
 // device's resident block slots.  Cost model, in units of one block's full-protein time:
 //   rounds(S) / S * (1 + 0.01 * (S - 1))
 // (rounds = ceil(blocks * S / slots); the small per-slice term covers the reduction and the
-// shorter protein loop of thin slices).  Slices keep at least 64 protein atoms.
+// shorter protein loop of thin slices).  Slices keep at least 64 protein atoms here; the measured
+// search below also tries thinner slices.
 int choose_split(const Context &c, bude_launch_cfg &cfg) {
   return choose_split_for(c.num_sms, c.natpro_pad, c.nposes, cfg);
 }
@@ -127,16 +128,53 @@ int autotune(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms) {
   float best_t = 1e30f;
   float budget = (float)std::max(max_ms, 1);
   float spent = 0.f;
-  for (const bude_launch_cfg &cfg : cands) {
-    float ms = 0.f;
-    rc = time_cfg(c, cfg, 2, &ms);
-    if (rc) break;
-    spent += 3.f * ms;
-    if (ms < best_t) {
-      best_t = ms;
+  auto trial = [&](const bude_launch_cfg &cfg, float *ms) {
+    rc = time_cfg(c, cfg, 2, ms);
+    if (rc) return false;
+    spent += 3.f * *ms;
+    if (*ms < best_t) {
+      best_t = *ms;
       best = cfg;
     }
-    if (spent > budget) break;
+    return spent <= budget;
+  };
+  // Phase 1: every shape with the wave model's split.
+  std::vector<std::pair<float, bude_launch_cfg>> timed;
+  for (const bude_launch_cfg &cfg : cands) {
+    float ms = 0.f;
+    const bool more = trial(cfg, &ms);
+    if (rc) break;
+    timed.push_back({ms, cfg});
+    if (!more) break;
+  }
+  // Phase 2: the four fastest global-reduce shapes over every distinct slice width from half to
+  // two and a half times the model's split (slices down to 32 atoms).  The model's rounds of
+  // resident blocks do not capture how much more resident warps per SM help: on 938 atoms x 65,536
+  // poses, 8 poses per thread, 128 threads, it picks 12 slices where 20 (48-atom slices) measured
+  // 6% faster.
+  if (!rc && spent <= budget) {
+    std::sort(timed.begin(), timed.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+    const int smax_thin = std::max(1, std::min(64, c.natpro_pad / 32));
+    int widened = 0;
+    for (const auto &t : timed) {
+      if (widened == 4 || rc || spent > budget) break;
+      const bude_launch_cfg base = t.second;
+      if (base.cluster != 0) continue;
+      ++widened;
+      int last_slice = -1;
+      for (int sp = std::max(2, base.split / 2); sp <= std::min(smax_thin, base.split * 5 / 2); ++sp) {
+        const int slice = (c.natpro_pad + sp - 1) / sp;
+        const int width = (slice + kAtomAlign - 1) / kAtomAlign * kAtomAlign;
+        if (width == last_slice || sp == base.split) continue;
+        // The fewest slices of this width (more would only add empty blocks).
+        if ((c.natpro_pad + width - 1) / width != sp) continue;
+        last_slice = width;
+        bude_launch_cfg cfg = base;
+        cfg.split = sp;
+        float ms = 0.f;
+        if (!trial(cfg, &ms) || rc) break;
+      }
+    }
   }
   c.natlig = natlig_full;
   if (rc) return rc;
