@@ -299,10 +299,11 @@ int bude_gpu_selftest_wait(bude_gpu_ctx *ctx, int32_t limit_us, float *elapsed_m
  * process exits: sizes above BUDE_NOALLOC_MAX_POSES poses or BUDE_NOALLOC_MAX_SLAB_RECORDS slab
  * records (forcefield types x protein atoms rounded up to 8) are rejected with BUDE_ERR_ARG.
  * Calls share that array: calls whose work overlaps on one GPU race and must be serialised by the
- * caller.  The first call on a device looks up the array's device address (cudaGetSymbolAddress)
- * and keeps it for the process: make that first call before any stream capture begins, and do not
- * use the entry point on a device after cudaDeviceReset.  Atom types outside the forcefield give
- * BUDE_ERR_TYPE and leave energies unwritten. */
+ * caller.  Every call is synchronous: it reads its status word back and waits for `stream`, so it
+ * cannot be recorded into a CUDA graph (inside a stream capture it fails and invalidates the
+ * capture).  The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * and keeps it for the process: do not use the entry point on a device after cudaDeviceReset.
+ * Atom types outside the forcefield give BUDE_ERR_TYPE and leave energies unwritten. */
 #define BUDE_NOALLOC_MAX_POSES 65536
 #define BUDE_NOALLOC_MAX_SLAB_RECORDS 131072
 int bude_gpu_fasten_noalloc(const bude_atom *protein, int32_t natpro, const bude_atom *ligand, int32_t natlig,
