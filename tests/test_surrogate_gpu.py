@@ -67,11 +67,22 @@ def test_tcgen05_and_mma_sync_scorers_agree(setup):
         ctx.surrogate_set_scorer("wmma")
 
 
-def test_gradient_matches_torch_autograd(setup):
-    ctx, batch = setup
-    rng = np.random.default_rng(0)
-    labels = rng.normal(50.0, 80.0, batch.total_poses).astype(np.float32)
-    poses = rng.choice(batch.total_poses, 300, replace=False).astype(np.int32)
+def poses_with_rows(batch, target, seed):
+    """Pose indices whose ligands' atom counts sum to exactly `target` rows."""
+    rng = np.random.default_rng(seed)
+    all_cnt = counts_of(batch, np.arange(batch.total_poses))
+    for _ in range(200):
+        picked, rows = [], 0
+        for p in rng.permutation(batch.total_poses):
+            if rows + all_cnt[p] <= target:
+                picked.append(p)
+                rows += all_cnt[p]
+            if rows == target:
+                return np.array(picked, np.int32)
+    raise AssertionError(f"no pose set of {target} rows")
+
+
+def assert_gradient_matches_torch(ctx, batch, poses, labels):
     grads, pred = ctx.surrogate_gradient(poses, labels)
     cnt = counts_of(batch, poses)
     X, types = ctx.surrogate_features(poses, int(cnt.sum()))
@@ -92,6 +103,31 @@ def test_gradient_matches_torch_autograd(setup):
             g_gpu, g_ref = g_gpu[:1], g_ref[:1]
         rels[name] = float(np.linalg.norm(g_gpu - g_ref) / max(np.linalg.norm(g_ref), 1e-12))
     assert max(rels.values()) < 0.05, rels
+
+
+def test_gradient_matches_torch_autograd(setup):
+    ctx, batch = setup
+    rng = np.random.default_rng(0)
+    labels = rng.normal(50.0, 80.0, batch.total_poses).astype(np.float32)
+    poses = rng.choice(batch.total_poses, 300, replace=False).astype(np.int32)
+    assert_gradient_matches_torch(ctx, batch, poses, labels)
+
+
+@pytest.mark.parametrize("rows", [256, 129, 127])
+def test_gradient_at_tile_edges(setup, rows):
+    """The training pass keeps its rows in 128-row tiles: whole tiles, one row into a second tile,
+    and a single partial tile give the same gradients as the FP32 reference."""
+    ctx, batch = setup
+    labels = np.random.default_rng(1).normal(50.0, 80.0, batch.total_poses).astype(np.float32)
+    poses = poses_with_rows(batch, rows, seed=rows)
+    assert counts_of(batch, poses).sum() == rows
+    assert_gradient_matches_torch(ctx, batch, poses, labels)
+
+
+def test_gradient_of_one_pose(setup):
+    ctx, batch = setup
+    labels = np.random.default_rng(2).normal(50.0, 80.0, batch.total_poses).astype(np.float32)
+    assert_gradient_matches_torch(ctx, batch, np.array([17], np.int32), labels)
 
 
 def test_training_reduces_loss_deterministically_and_checkpoints(built_library, tmp_path):
