@@ -7,10 +7,14 @@
 //   layers    z1 = W1 x + b1 (128), h1 = act(z1); z2 = W2 h1 + b2, h2 = act(z2);
 //             z3 = W3 h2 + b3, h3 = act(z3); y = w4 . h3 + b4,   act = hard-swish (mlp.cuh)
 //   pose      E_pose = sum over the ligand's atoms of y
-// Weights W1..W3 and the embedding are BF16 on the device for the tensor cores (FP32 masters and
-// FP32 Adam state are kept beside them); activations are rounded to BF16 between layers; every
-// product accumulates in FP32 (mma.sync m16n8k16).  Weights are stored [out][in] (in contiguous),
-// so a layer's B fragments are plain ldmatrix loads; the backward pass uses transposed copies.
+// FP32 masters and FP32 Adam state; 16-bit copies for the tensor cores: BF16 (plain and
+// transposed) for training and for the warp-level mma.sync scorer in this file, FP16 for the
+// tcgen05 scorer (score_tc.cuh).  Activations between hidden layers are rounded to the 16-bit type;
+// every product accumulates in FP32.  Weights are stored [out][in] (in contiguous), so a layer's
+// mma.sync B fragments are plain ldmatrix loads and a tcgen05 operand tile is a K-major copy.
+// This file holds the field grid, the features, the mma.sync scorer (`score_kernel`, selectable
+// through bude_surrogate_set_scorer) and the training pass's small kernels; the training GEMMs are
+// in score_tc.cuh (forward, backward) and wgrad_tc.cuh (weight gradients).
 //
 // The protein-field channels come from a grid precomputed once per protein (grid_kernel): for a
 // point x and protein atoms p (radius R_p, hphb h_p, elsc q_p, hbtype), distance r = |x - p|:
