@@ -181,8 +181,9 @@ int bude_gpu_download_batch(bude_gpu_ctx *ctx, float *energies, int64_t total_po
  * learned type embedding, the transformed atom position and 13 protein-field channels sampled
  * from a grid precomputed for the protein -- go through 32 -> 128 -> 128 -> 128 -> 1 with
  * hard-swish activations (h = z * sat(z/6 + 1/2), the piecewise-polynomial form of SiLU); the
- * outputs are summed per pose.  BF16 weights on BF16 tensor-core GEMMs with FP32 accumulation;
- * FP32 master weights and Adam state. */
+ * outputs are summed per pose.  Training runs BF16 tensor-core GEMMs (tcgen05) with FP32
+ * accumulation, FP32 master weights and Adam state; the default scorer runs FP16 tensor-core GEMMs
+ * with FP32 accumulation. */
 #define BUDE_SURROGATE_NPARAMS 38404
 
 /* Create (or reset) the context's surrogate for a protein: builds the field grid over
@@ -207,8 +208,9 @@ int bude_surrogate_download(bude_gpu_ctx *ctx, float *scores, int64_t n);
 
 /* Which kernel scores poses (bude_surrogate_score and the screening pipeline):
  * BUDE_SCORER_TCGEN05 (default) runs the three hidden layers as tcgen05 UMMAs with TMEM
- * accumulators; BUDE_SCORER_MMA_SYNC runs them as warp-level mma.sync.  Both evaluate the same
- * network with the same BF16 roundings; they differ only in FP32 summation order. */
+ * accumulators, in FP16; BUDE_SCORER_MMA_SYNC runs them as warp-level mma.sync in BF16, the
+ * roundings of the training pass.  Both evaluate the same network and accumulate in FP32; their
+ * scores differ by the 16-bit roundings of the activations (a few tenths of a per cent). */
 #define BUDE_SCORER_TCGEN05 0
 #define BUDE_SCORER_MMA_SYNC 1
 int bude_surrogate_set_scorer(bude_gpu_ctx *ctx, int32_t scorer);
