@@ -351,7 +351,8 @@ def run_ours(args, dist: Dist):
         out["e2e"] = {"value": round(dist.world * interactions / e2e_s / 1e9, 3), "unit": UNIT,
                       "h2d_bytes_per_step": int(deck.poses.nbytes + (0 if streamed else deck.ligand.nbytes)),
                       "d2h_bytes_per_step": int(deck.nposes * 4), "ms_per_step": round(e2e_s * 1e3, 4),
-                      "api": "bude_gpu_score_stream (chunks of 131,072 poses)" if streamed else "bude_gpu_score_host"}
+                      "api": ("bude_gpu_score_stream (chunks of 131,072 poses, rounded up by the library to whole waves "
+                              "of the launch)") if streamed else "bude_gpu_score_host"}
         pin_p.free()
         pin_e.free()
     ctx.close()

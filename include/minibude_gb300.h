@@ -133,8 +133,9 @@ int bude_gpu_score_host(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, const bud
  * H2D copy of src/cuda/fasten.hpp:256-270 for decks too large to stage at once or produced on the
  * host.  poses: six fields at poses + k*pose_stride (poses.in layout); energies: nposes floats.
  * Pinned host buffers (bude_host_alloc) let the copies overlap.  The energies equal those of
- * bude_gpu_run with the same cfg over all poses, bit for bit, for any chunk.  *ms (optional):
- * CUDA-event time of the whole call.  No counterpart in the reference. */
+ * bude_gpu_run with the same cfg over all poses, bit for bit, for any chunk.  The chunk is rounded
+ * up to whole waves of the launch shape's resident blocks (so each chunk's launch fills the GPU).
+ * *ms (optional): CUDA-event time of the whole call.  No counterpart in the reference. */
 int bude_gpu_score_stream(bude_gpu_ctx *ctx, const bude_launch_cfg *cfg, const float *poses, int64_t pose_stride,
                           int64_t nposes, int64_t chunk, float *energies, float *ms);
 

@@ -78,6 +78,17 @@ static int score_stream(Context &c, const bude_launch_cfg &cfg, const float *pos
   if (chunk <= 0) return set_error(BUDE_ERR_ARG, "chunk must be positive (got %lld)", chunk);
   int rc = check_cfg(c, cfg);
   if (rc) return rc;
+  {
+    // Round the chunk up to whole waves of the launch shape's resident blocks, so that no chunk's
+    // launch leaves SMs idle in a partial last wave (131,072 poses at 16 poses per thread, 128
+    // threads and 8 slices fill 0.84 of one wave of 608 blocks; 155,648 fill it).
+    int per_sm = 0;
+    if (exact_blocks_per_sm(cfg, &per_sm) == BUDE_OK && per_sm > 0) {
+      const long long slots = (long long)per_sm * std::max(c.num_sms, 1);
+      const long long ppw = std::max(1LL, slots / std::max(cfg.split, 1)) * cfg.ppwi * cfg.wgsize;
+      chunk = (chunk + ppw - 1) / ppw * ppw;
+    }
+  }
   chunk = std::min(chunk, std::max(nposes, 1LL));
   StreamState *sp = nullptr;
   rc = streamer(c, chunk, &sp);
