@@ -90,6 +90,16 @@ def test_ragged_pose_counts(ctx, n):
     assert_parity(ctx.download(), refs[:n], f64[:n])
 
 
+@pytest.mark.parametrize("split", [20, 24, 29, 64])
+def test_thin_protein_slices(ctx, split):
+    # The autotuner's second pass tries slices down to 32 atoms (938 atoms: 20 slices of 48, 24 of
+    # 40); 29 and 64 slices leave trailing blocks with no atoms, which must add nothing.
+    deck, refs, f64 = load_golden("small_head")
+    ctx.upload(deck)
+    ctx.run(launch_cfg(8, 128, split, 64, 2, cluster=0))
+    assert_parity(ctx.download(), refs, f64)
+
+
 def test_bm2_all_splits(ctx):
     deck, refs, f64 = load_golden("bm2_head")
     ctx.upload(deck)
