@@ -224,13 +224,20 @@ int check_cfg(const Context &c, const bude_launch_cfg &cfg) {
   return BUDE_OK;
 }
 
+// The compilation of exact_kernel<P, U> a block size runs: the narrow one (170 registers) for
+// blocks of at most kNarrowThreads threads.
+template <int P, int U> static decltype(&exact_kernel<P, U>) exact_entry(int wgsize) {
+  return wgsize <= kNarrowThreads ? exact_kernel_narrow<P, U> : exact_kernel<P, U>;
+}
+
 template <int P, int U>
 static cudaError_t launch_exact_pu(const ExactArgs &a, dim3 grid, int wgsize, size_t smem, int split,
                                    cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(exact_kernel<P, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const auto kernel = exact_entry<P, U>(wgsize);
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (split == 1 || !a.cluster) {
-    exact_kernel<P, U><<<grid, wgsize, smem, st>>>(a);
+    kernel<<<grid, wgsize, smem, st>>>(a);
     return cudaGetLastError();
   }
   cudaLaunchConfig_t lc = {};
@@ -245,7 +252,7 @@ static cudaError_t launch_exact_pu(const ExactArgs &a, dim3 grid, int wgsize, si
   attr[0].val.clusterDim.z = 1;
   lc.attrs = attr;
   lc.numAttrs = 1;
-  return cudaLaunchKernelEx(&lc, exact_kernel<P, U>, a);
+  return cudaLaunchKernelEx(&lc, kernel, a);
 }
 
 template <int P>
@@ -259,8 +266,9 @@ static cudaError_t launch_exact_p(const ExactArgs &a, dim3 grid, const bude_laun
 }
 
 template <int P, int U> static int blocks_per_sm_pu(int wgsize, size_t smem, int *out) {
-  cudaError_t e = cudaFuncSetAttribute(exact_kernel<P, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, exact_kernel<P, U>, wgsize, smem);
+  const auto kernel = exact_entry<P, U>(wgsize);
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kernel, wgsize, smem);
   return e == cudaSuccess ? BUDE_OK : cuda_error(e, "occupancy query");
 }
 

@@ -180,8 +180,7 @@ template <int P> struct PosePairs {
 };
 
 // P poses per thread; U protein atoms per unrolled inner-loop body.
-template <int P, int U>
-__global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
+template <int P, int U> __device__ __forceinline__ void exact_body(const ExactArgs &a) {
   extern __shared__ __align__(128) unsigned char smem[];
   float4 *stages = reinterpret_cast<float4 *>(smem);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)kStages * a.tile * kRecF4 * sizeof(float4));
@@ -288,6 +287,16 @@ __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
     }
   }
   cluster.sync();
+}
+
+// The kernel for every block size up to kMaxThreads (128 registers per thread), and the same
+// kernel compiled for blocks of at most kNarrowThreads threads, kNarrowBlocks per SM (170).
+template <int P, int U> __global__ void __launch_bounds__(kMaxThreads) exact_kernel(const ExactArgs a) {
+  exact_body<P, U>(a);
+}
+template <int P, int U>
+__global__ void __launch_bounds__(kNarrowThreads, kNarrowBlocks) exact_kernel_narrow(const ExactArgs a) {
+  exact_body<P, U>(a);
 }
 
 } // namespace bude
