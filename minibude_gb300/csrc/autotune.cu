@@ -154,7 +154,9 @@ int autotune(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms) {
   // 6% faster.
   if (!rc && spent <= budget) {
     std::sort(timed.begin(), timed.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
-    const int smax_thin = std::max(1, std::min(64, c.natpro_pad / 32));
+    // Splits whose slice sums ([split][nposes] floats) would pass 512 MB are not tried.
+    const long long split_cap = std::max(1LL, (512LL << 20) / (4LL * std::max(c.nposes, 1LL)));
+    const int smax_thin = (int)std::max(1LL, std::min({64LL, (long long)c.natpro_pad / 32, split_cap}));
     int widened = 0;
     for (const auto &t : timed) {
       if (widened == 4 || rc || spent > budget) break;
@@ -174,6 +176,12 @@ int autotune(Context &c, int max_ms, bude_launch_cfg &best, float *best_ms) {
         float ms = 0.f;
         if (!trial(cfg, &ms) || rc) break;
       }
+    }
+    // A shape of this pass whose slice sums did not fit in device memory (a failed allocation)
+    // ends the pass; the pick stays the best shape timed so far.  Other errors are returned.
+    if (rc == BUDE_ERR_CUDA) {
+      (void)cudaGetLastError();
+      rc = BUDE_OK;
     }
   }
   c.natlig = natlig_full;
