@@ -412,7 +412,9 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
 //                                                   copies W3^T, W2^T, FP32 accumulators in TMEM)
 // Each dz is rounded to BF16, stored (row-tiled, the gradient kernel of wgrad_tc.cuh reads them)
 // and written into `act` as the next UMMA's A operand.  Rows past the end have dy = 0, so their
-// dz are exactly zero.  The pass streams the pre-activations once, so a thread keeps its row's
+// dz are exactly zero.  The element-wise work runs on BF16 pairs (mlp.cuh act_grad_bf16x2,
+// mul_bf16x2: the stored z are BF16 already), about half the instructions of the FP32 form on
+// the groups' critical path.  The pass streams the pre-activations once, so a thread keeps its row's
 // whole z_l (256 bytes) in registers: the 16 loads of a layer are in flight together, and those of
 // z2 and z1 are issued while the UMMA before them runs.  Three groups per block leave each thread
 // the registers for that (a fourth would cap it at 128).
@@ -422,7 +424,7 @@ template <int G> struct TcBwdSmem {
   alignas(128) unsigned char w3t[kHid * kHid * 2]; // W3^T: [in 128][out 128], K-major (K = out)
   alignas(128) unsigned char w2t[kHid * kHid * 2]; // W2^T
   alignas(128) unsigned char act[G][kHid * kHid * 2];
-  alignas(16) float w4f[kHid];
+  alignas(16) uint32_t w4h[kHid / 2]; // output weights as BF16 pairs
   alignas(8) uint64_t bar[G];
   int item[G];
   uint32_t tmem;
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(kBwdGroups * kTcGroupThreads, 1) train_backwar
 
   to_kmajor(s.w3t, A.w3t, kHid, kHid);
   to_kmajor(s.w2t, A.w2t, kHid, kHid);
-  for (int i = tid; i < kHid; i += blockDim.x) s.w4f[i] = __ldg(&A.w4[i]);
+  for (int i = tid; i < kHid / 2; i += blockDim.x) s.w4h[i] = pack_bf16(__ldg(&A.w4[2 * i]), __ldg(&A.w4[2 * i + 1]));
   if (tid == 0) {
     for (int q = 0; q < G; ++q) mbar_init(&s.bar[q], 1);
     mbar_fence_init();
@@ -532,10 +534,9 @@ __global__ void __launch_bounds__(kBwdGroups * kTcGroupThreads, 1) train_backwar
       const uint32_t *zw = reinterpret_cast<const uint32_t *>(&z[2 * c]);
       uint32_t d[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const float2 zz = unpack_bf16(zw[i]);
-        d[i] = pack_bf16(__uint_as_float(v[2 * i]) * act_grad(zz.x), __uint_as_float(v[2 * i + 1]) * act_grad(zz.y));
-      }
+      for (int i = 0; i < 8; ++i)
+        d[i] = mul_bf16x2(pack_bf16(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1])),
+                          act_grad_bf16x2(zw[i]));
       put16(dZ, row, c * 16, d, to_act);
     });
   };
@@ -549,18 +550,15 @@ __global__ void __launch_bounds__(kBwdGroups * kTcGroupThreads, 1) train_backwar
     const bool valid = row < A.rows;
     uint4 z[16];
     const float dy = valid ? A.dy[row] : 0.f;
+    const uint32_t dy2 = pack_bf16(dy, dy);
     load_row128(A.Z3, row, z);
-    // dz3 = dy * w4 * act'(z3)
+    // dz3 = dy * w4 * act'(z3), in packed BF16 (w4 as BF16 pairs)
 #pragma unroll
     for (int c = 0; c < kHid / 32; ++c) {
       const uint32_t *zw = reinterpret_cast<const uint32_t *>(&z[4 * c]);
       uint32_t d[16];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const float2 zz = unpack_bf16(zw[i]);
-        const int f = c * 32 + 2 * i;
-        d[i] = pack_bf16(dy * s.w4f[f] * act_grad(zz.x), dy * s.w4f[f + 1] * act_grad(zz.y));
-      }
+      for (int i = 0; i < 16; ++i) d[i] = mul_bf16x2(mul_bf16x2(dy2, s.w4h[c * 16 + i]), act_grad_bf16x2(zw[i]));
       put(A.dZ3, row, c * 32, d, true);
     }
     product_issue(smem_u32(s.w3t));
