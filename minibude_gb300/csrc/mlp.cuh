@@ -102,6 +102,17 @@ __device__ __forceinline__ uint32_t mul_bf16x2(uint32_t a, uint32_t b) {
   return d;
 }
 
+// The activation of a BF16 pair in packed BF16 arithmetic, three instructions: s = min(relu(z * c
+// + 1/2), 1) with c = 1/6 rounded to BF16 (0.16699), h = z * s.  The weight-gradient kernel
+// rebuilds the forward pass's activations from the stored pre-activations this way.
+__device__ __forceinline__ uint32_t act_bf16x2(uint32_t z) {
+  uint32_t t, h;
+  asm("fma.rn.relu.bf16x2 %0, %1, %2, %3;" : "=r"(t) : "r"(z), "r"(0x3E2B3E2Bu), "r"(0x3F003F00u));
+  asm("min.bf16x2 %0, %1, %2;" : "=r"(t) : "r"(t), "r"(0x3F803F80u));
+  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h) : "r"(z), "r"(t));
+  return h;
+}
+
 // dh/dz of a BF16 pair as a BF16 pair, five packed instructions: t = z * c + 1/2 with c = 1/3
 // rounded to BF16 (0.33398, 0.2% steep), kept where -3 < z < 3; 1 where z >= 3; 0 where z <= -3
 // (set.* gives 1.0 or 0.0 per half: act' = t * (gt(-3) - ge(3)) + ge(3)).

@@ -6,7 +6,7 @@
 //   dW3 = dZ3^T H2,  db3 = dZ3^T 1,   dW2 = dZ2^T H1,  db2 = dZ2^T 1,
 //   dW1 = dZ1^T X,   db1 = dZ1^T 1,   S = dZ1^T T  (T = one-hot of each row's atom type),
 //   dw4 = H3^T dy,
-// with H_l = act(Z_l) rounded to BF16 as the forward pass used it.  Each is one UMMA chain with the
+// with H_l = act(Z_l) rebuilt from the stored BF16 pre-activations (mlp.cuh act_bf16x2).  Each is one UMMA chain with the
 // rows as K: D[M = 128][N] += A[M][K = 16 rows] * B[N][K = 16 rows]^T, the operands staged in
 // shared memory in the MN-major core-matrix layout (M or N contiguous: a row's features go in as
 // 16-byte stores), the accumulators held in TMEM for the whole launch:
@@ -97,10 +97,7 @@ __device__ __forceinline__ void wg_store_half(unsigned char *tile, int nmn, int 
     if (apply_act) {
       uint32_t *w = reinterpret_cast<uint32_t *>(&v[q]);
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const float2 f = unpack_bf16(w[e]);
-        w[e] = act_pair(f.x, f.y); // act(0) = 0: rows past the end stay zero
-      }
+      for (int e = 0; e < 4; ++e) w[e] = act_bf16x2(w[e]); // act(0) = 0: rows past the end stay zero
     }
     *reinterpret_cast<uint4 *>(tile + mnmajor_offset(h * 64 + q * 8, k, nmn)) = v[q];
   }
