@@ -391,9 +391,9 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     const int grid = std::max(1, std::min((ftiles + kTcGroups - 1) / kTcGroups, std::max(c.num_sms, 1)));
     train_forward_tc_kernel<<<grid, kTcGroups * kTcGroupThreads, sizeof(TcSmem<kTcGroups>), c.stream>>>(f);
   }
-  train_loss_kernel<<<(nb + 127) / 128, 128, 0, c.stream>>>(m, s.y.as<float>(), p + kOffB4, s.labels.as<float>(),
-                                                          s.pred.as<float>(), s.loss.as<float>(), s.dy.as<float>(),
-                                                          s.dsum.as<float>(), 1.f / (float)nb);
+  train_loss_kernel<<<(nb + kLossPoses - 1) / kLossPoses, 32 * kLossPoses, 0, c.stream>>>(
+      m, s.y.as<float>(), p + kOffB4, s.labels.as<float>(), s.pred.as<float>(), s.loss.as<float>(), s.dy.as<float>(),
+      s.dsum.as<float>(), 1.f / (float)nb);
   {
     // Backward through the hidden layers on the tensor cores (score_tc.cuh): dz3, dz2, dz1 as BF16.
     cudaMemsetAsync(s.next.ptr, 0, sizeof(unsigned int), c.stream);
@@ -450,7 +450,7 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   reduce(part + kWgOffB1, wg_grid, kHid, kWgPart, gr + kOffB1);
   reduce(part + kWgOffW4, wg_grid, kHid, kWgPart, gr + kOffW4);
   reduce(part + kWgOffS, wg_grid, kHid * kMaxTypes, kWgPart, s.S_sum.as<float>());
-  reduce(s.dsum.as<float>(), (nb + 127) / 128, 1, 1, gr + kOffB4);
+  reduce(s.dsum.as<float>(), (nb + kLossPoses - 1) / kLossPoses, 1, 1, gr + kOffB4);
   reduce_segments_kernel<<<(unsigned)((red.first[red.nseg] + 31) / 32), 32 * kReduceWarps, 0, c.stream>>>(red);
   emb_grad_kernel<<<(kMaxTypes * kEmb * 32 + 255) / 256, 256, 0, c.stream>>>(s.S_sum.as<float>(),
                                                                        s.w1_bf.as<__nv_bfloat16>(), gr + kOffEmb);

@@ -402,35 +402,46 @@ __global__ void __launch_bounds__(256) train_features_kernel(MlpWeights W, Field
 // Per batch pose: prediction = sum of its rows' y + natlig * b4; loss on the compressed scale
 // c(E) = S * asinh(E / S); dy (per row) = dLoss/dprediction.  loss_out[i] = the pose's squared
 // error (summed on the host, deterministic); dsum[block] = the sum of dy over the block's rows.
+// One warp per pose (lanes take rows a, a + 32, ...; a butterfly sum gives every lane the total),
+// so a warp's row loads and dy stores are consecutive floats; kLossPoses warps per block keep the
+// number of dsum parts that the gradient reduction folds small.
 constexpr float kLossScale = 20.f;
+constexpr int kLossPoses = 32; // warps (poses) per block
 
-__global__ void __launch_bounds__(128) train_loss_kernel(RowMap m, const float *y, const float *b4,
-                                                         const float *labels, float *pred, float *loss_out, float *dy,
-                                                         float *dsum, float inv_batch) {
-  __shared__ float share[128];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  share[threadIdx.x] = 0.f;
+__global__ void __launch_bounds__(32 * kLossPoses) train_loss_kernel(RowMap m, const float *y, const float *b4,
+                                                                     const float *labels, float *pred,
+                                                                     float *loss_out, float *dy, float *dsum,
+                                                                     float inv_batch) {
+  __shared__ float share[kLossPoses];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = blockIdx.x * kLossPoses + warp;
+  float mine = 0.f;
   if (i < m.nposes) {
-    const int p = m.pose[i];
     const int row0 = m.row_off[i], n = m.row_off[i + 1] - row0;
     float s = 0.f;
-    for (int a = 0; a < n; ++a) s += y[row0 + a];
+    for (int a = lane; a < n; a += 32) s += y[row0 + a];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     s += n * b4[0];
-    pred[i] = s;
-    const float cs = kLossScale * asinhf(s / kLossScale), ce = kLossScale * asinhf(labels[p] / kLossScale);
+    const float cs = kLossScale * asinhf(s / kLossScale), ce = kLossScale * asinhf(labels[m.pose[i]] / kLossScale);
     const float d = cs - ce;
-    loss_out[i] = d * d;
     const float grad = 2.f * d * rsqrtf(1.f + (s / kLossScale) * (s / kLossScale)) * inv_batch;
-    for (int a = 0; a < n; ++a) dy[row0 + a] = grad;
-    share[threadIdx.x] = (float)n * grad; // the pose's share of the b4 gradient (sum of dy over its rows)
+    for (int a = lane; a < n; a += 32) dy[row0 + a] = grad;
+    if (lane == 0) {
+      pred[i] = s;
+      loss_out[i] = d * d;
+    }
+    mine = (float)n * grad; // the pose's share of the b4 gradient (sum of dy over its rows)
   }
-  // dsum[block] = the block's poses' shares, summed in a fixed tree order
+  if (lane == 0) share[warp] = mine;
   __syncthreads();
-  for (int o = 64; o > 0; o >>= 1) {
-    if (threadIdx.x < o) share[threadIdx.x] += share[threadIdx.x + o];
-    __syncthreads();
+  // dsum[block] = the block's poses' shares in a fixed butterfly order
+  if (warp == 0) {
+    float t = share[lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) dsum[blockIdx.x] = t;
   }
-  if (threadIdx.x == 0) dsum[blockIdx.x] = share[0];
 }
 
 // The per-step gradient reductions in one launch: segment k sums parts [0, nparts) of
