@@ -289,12 +289,13 @@ __global__ void __launch_bounds__(kTcGroups * kTcGroupThreads, 1) train_forward_
   const int tid = threadIdx.x, g = tid / kTcGroupThreads, lt = tid % kTcGroupThreads;
   const uint32_t bar_id = 1 + g;
 
-  tc_setup<false>(s, tc_weights(A.W));
   if (tid == 0) {
     for (int q = 0; q < G; ++q) mbar_init(&s.bar[q], 1);
     mbar_fence_init();
   }
   if (tid < 32) tmem_alloc<tc_alloc_cols<G>()>(&s.tmem);
+  grid_dep_wait(); // the setup above may overlap the features kernel; the weights and X come after
+  tc_setup<false>(s, tc_weights(A.W));
   fence_proxy_async();
   tc_fence_before();
   __syncthreads();
@@ -457,14 +458,15 @@ __global__ void __launch_bounds__(kBwdGroups * kTcGroupThreads, 1) train_backwar
   const int tid = threadIdx.x, g = tid / kTcGroupThreads, lt = tid % kTcGroupThreads;
   const uint32_t bar_id = 1 + g;
 
-  to_kmajor(s.w3t, A.w3t, kHid, kHid);
-  to_kmajor(s.w2t, A.w2t, kHid, kHid);
-  for (int i = tid; i < kHid / 2; i += blockDim.x) s.w4h[i] = pack_bf16(__ldg(&A.w4[2 * i]), __ldg(&A.w4[2 * i + 1]));
   if (tid == 0) {
     for (int q = 0; q < G; ++q) mbar_init(&s.bar[q], 1);
     mbar_fence_init();
   }
   if (tid < 32) tmem_alloc<tc_alloc_cols<G>()>(&s.tmem);
+  grid_dep_wait(); // the setup above may overlap the loss kernel; everything below reads its inputs
+  to_kmajor(s.w3t, A.w3t, kHid, kHid);
+  to_kmajor(s.w2t, A.w2t, kHid, kHid);
+  for (int i = tid; i < kHid / 2; i += blockDim.x) s.w4h[i] = pack_bf16(__ldg(&A.w4[2 * i]), __ldg(&A.w4[2 * i + 1]));
   fence_proxy_async();
   tc_fence_before();
   __syncthreads();

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <numeric>
 #include <random>
+#include <utility>
 #include <vector>
 
 #include "exact_kernel.cuh"
@@ -353,6 +354,27 @@ static int ensure_train_scratch(Surrogate &s, long long rows, int batch, int wg_
   return rc;
 }
 
+// Launch one kernel of a training step with programmatic stream serialisation: its blocks are
+// scheduled as the kernel before it finishes, and run their setup (barriers, TMEM allocation) until
+// grid_dep_wait (ptx.cuh) while that kernel's completion is processed.  Every kernel launched this
+// way waits before it touches the step's buffers.  80 epochs of 512 ligands x 4096 poses: 6.03 s
+// this way, 6.48 s in plain stream order.
+template <class... KArgs, class... Args>
+static cudaError_t launch_chained(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                                  cudaStream_t st, Args &&...args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // One optimisation step on `nb` poses whose indices/row offsets are at dpose/drowoff.
 static int train_step(Context &c, Surrogate &s, const int *dpose, const int *drowoff, int nb, long long rows, float lr,
                       float *loss_sum_dev_host) {
@@ -368,15 +390,16 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   // One gradient block per SM, each with at least one 128-row tile.
   const int wg_grid = (int)std::min<long long>((rows + kWgTile - 1) / kWgTile, std::max(c.num_sms, 1));
   int rc = ensure_train_scratch(s, rows, nb, wg_grid);
+  if (!rc) rc = s.next.reserve(256, "work counters");
   if (rc) return rc;
-  train_features_kernel<<<(nb * 32 + 255) / 256, 256, 0, c.stream>>>(W, s.fg, c.b_ligands.as<float4>(),
-                                                                       c.b_xform.as<float4>(), m,
-                                                                       s.X.as<__nv_bfloat16>(), s.row_type.as<int>());
+  // The step's kernels run as one chain of programmatic dependent launches (launch_chained); the
+  // features kernel zeroes the forward (next[0]) and backward (next[1]) tile counters.
+  unsigned int *counters = s.next.as<unsigned int>();
+  cudaError_t le = launch_chained(train_features_kernel, (unsigned)((nb * 32 + 255) / 256), 256u, 0, c.stream, W,
+                                  s.fg, c.b_ligands.as<float4>(), c.b_xform.as<float4>(), m,
+                                  s.X.as<__nv_bfloat16>(), s.row_type.as<int>(), counters);
   {
     // Forward on the tensor cores (score_tc.cuh): z1, z2, z3 as BF16 and y per row.
-    rc = s.next.reserve(256, "work counter");
-    if (rc) return rc;
-    cudaMemsetAsync(s.next.ptr, 0, sizeof(unsigned int), c.stream);
     TrainFwdTcArgs f;
     f.W = W;
     f.X = s.X.as<__nv_bfloat16>();
@@ -386,17 +409,19 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     f.Z3 = s.Z3.as<__nv_bfloat16>();
     f.y = s.y.as<float>();
     f.err = c.err.as<unsigned int>();
-    f.next = s.next.as<unsigned int>();
+    f.next = counters;
     const int ftiles = (int)((rows + kTcGroupThreads - 1) / kTcGroupThreads);
     const int grid = std::max(1, std::min((ftiles + kTcGroups - 1) / kTcGroups, std::max(c.num_sms, 1)));
-    train_forward_tc_kernel<<<grid, kTcGroups * kTcGroupThreads, sizeof(TcSmem<kTcGroups>), c.stream>>>(f);
+    if (le == cudaSuccess)
+      le = launch_chained(train_forward_tc_kernel, (unsigned)grid, (unsigned)(kTcGroups * kTcGroupThreads),
+                          sizeof(TcSmem<kTcGroups>), c.stream, f);
   }
-  train_loss_kernel<<<(nb + kLossPoses - 1) / kLossPoses, 32 * kLossPoses, 0, c.stream>>>(
-      m, s.y.as<float>(), p + kOffB4, s.labels.as<float>(), s.pred.as<float>(), s.loss.as<float>(), s.dy.as<float>(),
-      s.dsum.as<float>(), 1.f / (float)nb);
+  if (le == cudaSuccess)
+    le = launch_chained(train_loss_kernel, (unsigned)((nb + kLossPoses - 1) / kLossPoses), 32u * kLossPoses, 0,
+                        c.stream, m, s.y.as<float>(), p + kOffB4, s.labels.as<float>(), s.pred.as<float>(),
+                        s.loss.as<float>(), s.dy.as<float>(), s.dsum.as<float>(), 1.f / (float)nb);
   {
     // Backward through the hidden layers on the tensor cores (score_tc.cuh): dz3, dz2, dz1 as BF16.
-    cudaMemsetAsync(s.next.ptr, 0, sizeof(unsigned int), c.stream);
     TrainBwdTcArgs b;
     b.w3t = s.w3t_bf.as<__nv_bfloat16>();
     b.w2t = s.w2t_bf.as<__nv_bfloat16>();
@@ -410,10 +435,12 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     b.dZ2 = s.dZ2.as<__nv_bfloat16>();
     b.dZ3 = s.dZ3.as<__nv_bfloat16>();
     b.err = c.err.as<unsigned int>();
-    b.next = s.next.as<unsigned int>();
+    b.next = counters + 1;
     const int btiles = (int)((rows + kTcGroupThreads - 1) / kTcGroupThreads);
     const int grid = std::max(1, std::min((btiles + kBwdGroups - 1) / kBwdGroups, std::max(c.num_sms, 1)));
-    train_backward_tc_kernel<<<grid, kBwdGroups * kTcGroupThreads, sizeof(TcBwdSmem<kBwdGroups>), c.stream>>>(b);
+    if (le == cudaSuccess)
+      le = launch_chained(train_backward_tc_kernel, (unsigned)grid, (unsigned)(kBwdGroups * kTcGroupThreads),
+                          sizeof(TcBwdSmem<kBwdGroups>), c.stream, b);
   }
   // Weight, bias and embedding gradients on the tensor cores (wgrad_tc.cuh): per-block partial
   // sums over contiguous row tiles, folded in block order.
@@ -430,7 +457,8 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   w.rows = (int)rows;
   w.part = s.part_w.as<float>();
   w.err = c.err.as<unsigned int>();
-  wgrad_tc_kernel<<<wg_grid, kWgThreads, sizeof(WgTcSmem), c.stream>>>(w);
+  if (le == cudaSuccess)
+    le = launch_chained(wgrad_tc_kernel, (unsigned)wg_grid, (unsigned)kWgThreads, sizeof(WgTcSmem), c.stream, w);
   ReduceSegs red{};
   auto reduce = [&](const float *part, int nparts, long long n, long long stride, float *dst) {
     const int k = red.nseg++;
@@ -451,18 +479,23 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   reduce(part + kWgOffW4, wg_grid, kHid, kWgPart, gr + kOffW4);
   reduce(part + kWgOffS, wg_grid, kHid * kMaxTypes, kWgPart, s.S_sum.as<float>());
   reduce(s.dsum.as<float>(), (nb + kLossPoses - 1) / kLossPoses, 1, 1, gr + kOffB4);
-  reduce_segments_kernel<<<(unsigned)((red.first[red.nseg] + 31) / 32), 32 * kReduceWarps, 0, c.stream>>>(red);
-  emb_grad_kernel<<<(kMaxTypes * kEmb * 32 + 255) / 256, 256, 0, c.stream>>>(s.S_sum.as<float>(),
-                                                                       s.w1_bf.as<__nv_bfloat16>(), gr + kOffEmb);
+  if (le == cudaSuccess)
+    le = launch_chained(reduce_segments_kernel, (unsigned)((red.first[red.nseg] + 31) / 32), 32u * kReduceWarps, 0,
+                        c.stream, red);
+  if (le == cudaSuccess)
+    le = launch_chained(emb_grad_kernel, (unsigned)((kMaxTypes * kEmb * 32 + 255) / 256), 256u, 0, c.stream,
+                        s.S_sum.as<float>(), s.w1_bf.as<__nv_bfloat16>(), gr + kOffEmb);
   if (lr > 0.f) {
     s.step++;
     s.w4_host_valid = false;
     const float b1 = 0.9f, b2 = 0.999f;
     const double bc1 = 1.0 - std::pow((double)b1, (double)s.step), bc2 = 1.0 - std::pow((double)b2, (double)s.step);
-    adam_kernel<<<(unsigned)((kNParams + 255) / 256), 256, 0, c.stream>>>(
-        s.params.as<float>(), s.adam_m.as<float>(), s.adam_v.as<float>(), gr, kNParams, (float)(lr / bc1),
-        (float)std::sqrt(bc2), b1, b2, 1e-8f, bf_copies(s));
+    if (le == cudaSuccess)
+      le = launch_chained(adam_kernel, (unsigned)((kNParams + 255) / 256), 256u, 0, c.stream, s.params.as<float>(),
+                          s.adam_m.as<float>(), s.adam_v.as<float>(), (const float *)gr, (long long)kNParams,
+                          (float)(lr / bc1), (float)std::sqrt(bc2), b1, b2, 1e-8f, bf_copies(s));
   }
+  if (le != cudaSuccess) return cuda_error(le, "surrogate training step launch");
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "surrogate training step");
   (void)loss_sum_dev_host;
@@ -685,7 +718,8 @@ int surrogate_features(Context &c, const int *poses, int n, float *X, int *types
   m.nposes = n;
   train_features_kernel<<<(n * 32 + 255) / 256, 256, 0, c.stream>>>(weights(s), s.fg, c.b_ligands.as<float4>(),
                                                                       c.b_xform.as<float4>(), m,
-                                                                      s.X.as<__nv_bfloat16>(), s.row_type.as<int>());
+                                                                      s.X.as<__nv_bfloat16>(), s.row_type.as<int>(),
+                                                                      nullptr);
   e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return cuda_error(e, "surrogate features");
   std::vector<uint16_t> xb((size_t)tiled_rows(rows) * kFeat);

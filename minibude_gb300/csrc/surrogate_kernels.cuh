@@ -377,10 +377,13 @@ struct RowMap {
 };
 
 // One warp per batch pose writes the features (and types) of its rows; X is row-tiled (tc.cuh:
-// tiled_offset).
+// tiled_offset).  The first kernel of a training step: it also zeroes the step's two work counters
+// (`counters`, when given: the forward and backward passes' tile counters).
 __global__ void __launch_bounds__(256) train_features_kernel(MlpWeights W, FieldGrid g, const float4 *ligands,
                                                              const float4 *xform, RowMap m, __nv_bfloat16 *X,
-                                                             int *row_type) {
+                                                             int *row_type, unsigned int *counters) {
+  grid_dep_wait();
+  if (counters && blockIdx.x == 0 && threadIdx.x < 2) counters[threadIdx.x] = 0u;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= m.nposes) return;
@@ -412,6 +415,7 @@ __global__ void __launch_bounds__(32 * kLossPoses) train_loss_kernel(RowMap m, c
                                                                      const float *labels, float *pred,
                                                                      float *loss_out, float *dy, float *dsum,
                                                                      float inv_batch) {
+  grid_dep_wait();
   __shared__ float share[kLossPoses];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = blockIdx.x * kLossPoses + warp;
@@ -463,6 +467,7 @@ struct ReduceSegs {
 };
 
 __global__ void __launch_bounds__(32 * kReduceWarps) reduce_segments_kernel(const ReduceSegs r) {
+  grid_dep_wait();
   __shared__ float sums[kReduceWarps][32];
   const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
   const int e = blockIdx.x * 32 + lane;
@@ -524,6 +529,7 @@ __device__ __forceinline__ void bf_copy(const BfCopies &c, long long i, float w)
 // BF16 copies are written in the same pass.
 __global__ void adam_kernel(float *w, float *m, float *v, const float *grad, long long n, float step, float bc2_sqrt,
                             float b1, float b2, float eps, const BfCopies copies) {
+  grid_dep_wait();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float gr = grad[i];

@@ -124,6 +124,7 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs 
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  grid_dep_wait(); // the setup above may overlap the backward pass; its outputs are read below
   const uint32_t tmem = s.tmem;
   unsigned char *R = s.region;
   const uint32_t base = smem_u32(R);
@@ -302,6 +303,7 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs 
 // embedding entries; S summed over blocks already.  One warp per entry: lane l takes f = l, l + 32,
 // ..., and the lanes' sums are folded by a fixed butterfly, so the result is the same on every run.
 __global__ void emb_grad_kernel(const float *S, const __nv_bfloat16 *w1, float *demb) {
+  grid_dep_wait();
   const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = (int)(threadIdx.x & 31);
   if (i >= kMaxTypes * kEmb) return;
   const int t = i / kEmb, j = i % kEmb;
