@@ -458,7 +458,8 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   w.part = s.part_w.as<float>();
   w.err = c.err.as<unsigned int>();
   if (le == cudaSuccess)
-    le = launch_chained(wgrad_tc_kernel, (unsigned)wg_grid, (unsigned)kWgThreads, sizeof(WgTcSmem), c.stream, w);
+    le = launch_chained(wgrad_tc_kernel, (unsigned)wg_grid, (unsigned)(kWgThreads + 64), sizeof(WgTcSmem), c.stream,
+                        w);
   ReduceSegs red{};
   auto reduce = [&](const float *part, int nparts, long long n, long long stride, float *dst) {
     const int k = red.nseg++;

@@ -6,21 +6,28 @@
 //   dW3 = dZ3^T H2,  db3 = dZ3^T 1,   dW2 = dZ2^T H1,  db2 = dZ2^T 1,
 //   dW1 = dZ1^T X,   db1 = dZ1^T 1,   S = dZ1^T T  (T = one-hot of each row's atom type),
 //   dw4 = H3^T dy,
-// with H_l = act(Z_l) rebuilt from the stored BF16 pre-activations (mlp.cuh act_bf16x2).  Each is one UMMA chain with the
-// rows as K: D[M = 128][N] += A[M][K = 16 rows] * B[N][K = 16 rows]^T, the operands staged in
-// shared memory in the MN-major core-matrix layout (M or N contiguous: a row's features go in as
-// 16-byte stores), the accumulators held in TMEM for the whole launch:
-//   columns   0..143  dW3 | db3 (N = 128 + a ones column + 15 zero columns)
-//           144..287  dW2 | db2
-//           288..399  dW1 | S | db1 (N = 32 + 64 + 16)
-//           400..415  dw4 (N = 16: dy as two BF16 parts, hi + lo, and 14 zero columns)
+// with H_l = act(Z_l) rebuilt from the stored BF16 pre-activations (mlp.cuh act_bf16x2).  Each is
+// one UMMA chain with the rows as K: D[M = 128][N] += A[M][K = 16 rows] * B[N][K = 16 rows]^T, the
+// operands in shared memory in the MN-major core-matrix layout, the accumulators held in TMEM for
+// the whole launch:
+//   columns   0..127  dW3          128..255  dW2          256..351  dW1 | S (N = 32 + 64)
+//           352..367  dw4 (N = 16: dy as two BF16 parts, hi + lo, and 14 zero columns)
+//           368..383  db3, 384..399 db2, 400..415 db1 (dZ_l^T against a tile of ones, N = 16)
 // The embedding gradient follows as dEmb[t][j] = sum_f W1[f][j] S[f][t] (emb_grad_kernel).
 //
+// A 128-row tile of a row-tiled [rows][128] array (tc.cuh: tiled_offset) is byte for byte the
+// MN-major operand tile of these UMMAs, so the dZ and Z tiles reach shared memory as single 32 KB
+// TMA bulk copies, without registers.  Shared memory holds one slot per chain (224 KB in all):
+//   slot 3: dZ3 | Z2 -> H2     slot 2: dZ2 | Z1 -> H1     slot 1: dZ1 | X, T (built by threads)
+//   slot 4: Z3 -> H3 | dy (built by threads)               and the constant tile of ones.
+// Per tile the block runs the chains in the order 3, 2, 1, 4: wait for the slot's copies, rebuild
+// H in place (act) or write the thread-built operand, then one thread issues the chain's UMMAs and
+// commits them to the slot's "empty" barrier, and refills the slot of the chain before (whose UMMAs
+// were committed one chain earlier) with its next tile.  Every slot's next copies are therefore in
+// flight for three chains' time, about three quarters of a tile.  All waits are bounded.
+//
 // A block owns a contiguous range of 128-row tiles (the same on every run), so the partial sums
-// and their fixed-order reduction over blocks (reduce_segments_kernel) are deterministic.  Per
-// tile, phase A stages and issues layers 3 and 2, phase B layer 1 and the output weights, both in
-// one 136 KB region; a phase's UMMAs complete (bounded mbarrier wait) before the region is reused,
-// and the next phase's global loads are in flight while they run.
+// and their fixed-order reduction over blocks (reduce_segments_kernel) are deterministic.
 #pragma once
 #include <cstdint>
 
@@ -29,13 +36,13 @@
 
 namespace bude {
 
-constexpr int kWgTile = 128;     // rows per tile: K of 8 UMMAs
-constexpr int kWgThreads = 256;  // two threads per row when staging
-constexpr int kWgN3 = kHid + 16; // N of the layer-3 and layer-2 chains (features | ones | zeros)
-constexpr int kWgN1 = kFeat + kMaxTypes + 16; // N of the layer-1 chain (X | one-hot | ones | zeros)
-constexpr int kWgN4 = 16;        // N of the output-weight chain (dy hi | dy lo | zeros)
-constexpr int kWgCol3 = 0, kWgCol2 = kWgN3, kWgCol1 = 2 * kWgN3, kWgCol4 = 2 * kWgN3 + kWgN1;
-constexpr int kWgCols = kWgCol4 + kWgN4; // 416 TMEM columns used of the 512 allocated
+constexpr int kWgTile = 128;    // rows per tile: K of 8 UMMAs
+constexpr int kWgThreads = 256; // two threads per row for the thread-built operands
+constexpr int kWgN1 = kFeat + kMaxTypes; // N of the layer-1 chain (X | one-hot)
+constexpr int kWgNb = 16;                // N of the output-weight and bias chains
+constexpr int kWgCol3 = 0, kWgCol2 = kHid, kWgCol1 = 2 * kHid, kWgCol4 = kWgCol1 + kWgN1,
+              kWgColB3 = kWgCol4 + kWgNb, kWgColB2 = kWgColB3 + kWgNb, kWgColB1 = kWgColB2 + kWgNb;
+constexpr int kWgCols = kWgColB1 + kWgNb; // 416 TMEM columns used of the 512 allocated
 // Partial sums per block, floats: [dW3 128x128 | db3 128 | dW2 | db2 | dW1 128x32 | S 128x64 | db1 | dw4]
 constexpr int kWgOffW3 = 0, kWgOffB3 = kWgOffW3 + kHid * kHid, kWgOffW2 = kWgOffB3 + kHid,
               kWgOffB2 = kWgOffW2 + kHid * kHid, kWgOffW1 = kWgOffB2 + kHid, kWgOffS = kWgOffW1 + kHid * kFeat,
@@ -49,26 +56,30 @@ __host__ __device__ __forceinline__ uint32_t mnmajor_offset(int mn, int k, int n
   return (uint32_t)((mn >> 3) * 128 + (k >> 3) * (nmn / 8) * 128 + (k & 7) * 16 + (mn & 7) * 2);
 }
 constexpr uint32_t wg_tile_bytes(int nmn) { return (uint32_t)nmn * kWgTile * 2; }
+static_assert(wg_tile_bytes(kHid) == 128 * kHid * 2, "a [rows][128] tile is one operand tile");
 
-// Phase A: A3 = dZ3 [128], B3 = H2|1 [144], A2 = dZ2 [128], B2 = H1|1 [144].
-// Phase B: A1 = dZ1 [128], B1 = X|T|1 [112], A4 = H3 [128], B4 = dy [16].
-constexpr uint32_t kWgA3 = 0, kWgB3 = kWgA3 + wg_tile_bytes(kHid), kWgA2 = kWgB3 + wg_tile_bytes(kWgN3),
-                   kWgB2 = kWgA2 + wg_tile_bytes(kHid), kWgPhaseA = kWgB2 + wg_tile_bytes(kWgN3);
-constexpr uint32_t kWgA1 = 0, kWgB1 = kWgA1 + wg_tile_bytes(kHid), kWgA4 = kWgB1 + wg_tile_bytes(kWgN1),
-                   kWgB4 = kWgA4 + wg_tile_bytes(kHid), kWgPhaseB = kWgB4 + wg_tile_bytes(kWgN4);
-constexpr uint32_t kWgRegion = kWgPhaseA > kWgPhaseB ? kWgPhaseA : kWgPhaseB;
+constexpr int kWgChains = 4; // in processing order: layer 3, layer 2, layer 1, output weights
+constexpr int kWgCopies = 1; // bulk copies per 32 KB array tile
+constexpr uint32_t kWgZ = wg_tile_bytes(kHid); // 32 KB
+constexpr uint32_t kWgSlot3 = 0, kWgSlot2 = kWgSlot3 + 2 * kWgZ, kWgSlot1 = kWgSlot2 + 2 * kWgZ,
+                   kWgSlot4 = kWgSlot1 + kWgZ + wg_tile_bytes(kWgN1), kWgOnes = kWgSlot4 + kWgZ + wg_tile_bytes(kWgNb),
+                   kWgRegion = kWgOnes + wg_tile_bytes(kWgNb);
 
 struct WgTcSmem {
   alignas(128) unsigned char region[kWgRegion];
-  alignas(8) uint64_t bar;
+  alignas(8) uint64_t full[kWgChains];  // a slot's copies have landed (transaction bytes)
+  alignas(8) uint64_t ready[kWgChains]; // the workers have built the slot's operands (256 arrivals)
+  alignas(8) uint64_t empty[kWgChains]; // a slot's UMMAs have completed (tcgen05.commit)
   uint32_t tmem;
+  int abort;                            // set when a wait ran out: everyone leaves
 };
-static_assert(sizeof(WgTcSmem) <= 227 * 1024, "the staging region fits one block per SM");
+static_assert(sizeof(WgTcSmem) <= 227 * 1024, "the slots fit one block per SM");
 
 struct WgTcArgs {
   const __nv_bfloat16 *X;                // [rows][32], row-tiled (tc.cuh: tiled_offset)
   const int *row_type;                   // [rows]
-  const __nv_bfloat16 *Z1, *Z2, *Z3;     // [tiled_rows(rows)][128] pre-activations, row-tiled
+  const __nv_bfloat16 *Z1, *Z2, *Z3;     // [tiled_rows(rows)][128] pre-activations, row-tiled; every
+                                         // row of a tile finite (rows past the end: the biases)
   const __nv_bfloat16 *dZ1, *dZ2, *dZ3;  // [tiled_rows(rows)][128], row-tiled; zero past the end
   const float *dy;                       // [rows] (dy and row_type allocated for tiled_rows(rows))
   int rows;
@@ -81,25 +92,17 @@ __device__ __forceinline__ void wg_put(unsigned char *tile, int nmn, int f0, int
   *reinterpret_cast<uint4 *>(tile + mnmajor_offset(f0, k, nmn)) = v;
 }
 
-// The 64 features [h*64, h*64+64) of row r of a row-tiled [rows][128] BF16 array (every row of a
-// tile is written: rows past the end have zero gradients and finite pre-activations).
-__device__ __forceinline__ void wg_load_half(const __nv_bfloat16 *src, long long r, int h, uint4 (&v)[8]) {
-  const unsigned char *t = reinterpret_cast<const unsigned char *>(src) + tiled_offset(r, 0, kHid);
+// H = act(Z) in place over one 32 KB tile: 2,048 16-byte chunks, 8 per thread.
+__device__ __forceinline__ void wg_act_tile(unsigned char *tile) {
 #pragma unroll
-  for (int q = 0; q < 8; ++q) v[q] = __ldg(reinterpret_cast<const uint4 *>(t + kmajor_offset(0, h * 64 + q * 8, kHid)));
-}
-
-// Store them as row k of an MN-major tile, optionally through the activation (BF16 in, BF16 out).
-__device__ __forceinline__ void wg_store_half(unsigned char *tile, int nmn, int h, int k, uint4 (&v)[8],
-                                              bool apply_act) {
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    if (apply_act) {
-      uint32_t *w = reinterpret_cast<uint32_t *>(&v[q]);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) w[e] = act_bf16x2(w[e]); // act(0) = 0: rows past the end stay zero
-    }
-    *reinterpret_cast<uint4 *>(tile + mnmajor_offset(h * 64 + q * 8, k, nmn)) = v[q];
+  for (int i = 0; i < 8; ++i) {
+    uint4 *c = reinterpret_cast<uint4 *>(tile) + threadIdx.x + i * kWgThreads;
+    uint4 v = *c;
+    v.x = act_bf16x2(v.x);
+    v.y = act_bf16x2(v.y);
+    v.z = act_bf16x2(v.z);
+    v.w = act_bf16x2(v.w);
+    *c = v;
   }
 }
 
@@ -108,152 +111,202 @@ __device__ __forceinline__ uint32_t wg_idesc(int n) {
   return umma_idesc_bf16(kHid, n) | (1u << 15) | (1u << 16);
 }
 
-__global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs a) {
+__global__ void __launch_bounds__(kWgThreads + 64, 1) wgrad_tc_kernel(const WgTcArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   WgTcSmem &s = *reinterpret_cast<WgTcSmem *>(smem_raw);
-  const int tid = threadIdx.x, r = tid % kWgTile, h = tid / kWgTile; // row of the tile, half
+  const int tid = threadIdx.x, r = tid % kWgTile, h = (tid / kWgTile) & 1; // worker: row of the tile, half
+  // Warps 0-7: the workers (operand building); thread 0 of warp 8 issues the UMMAs, thread 0 of
+  // warp 9 issues the slot copies.
+  const bool worker = tid < kWgThreads, issuer = tid == kWgThreads, loader = tid == kWgThreads + 32;
   const int tiles = (a.rows + kWgTile - 1) / kWgTile;
   const int t0 = (int)((long long)tiles * blockIdx.x / gridDim.x);
   const int t1 = (int)((long long)tiles * (blockIdx.x + 1) / gridDim.x);
+  unsigned char *R = s.region;
 
   if (tid == 0) {
-    mbar_init(&s.bar, 1);
+    for (int j = 0; j < kWgChains; ++j) {
+      mbar_init(&s.full[j], 1);
+      mbar_init(&s.ready[j], kWgThreads);
+      mbar_init(&s.empty[j], 1);
+    }
+    s.abort = 0;
     mbar_fence_init();
   }
   if (tid < 32) tmem_alloc<512>(&s.tmem);
+  if (worker) {
+    // The tile of ones for the bias chains: B[n][k] = 1 for n = 0, 0 for n = 1..15.
+    const uint4 one_first = make_uint4(0x3F80u, 0u, 0u, 0u), zero = make_uint4(0u, 0u, 0u, 0u);
+    wg_put(R + kWgOnes, kWgNb, h * 8, r, h == 0 ? one_first : zero);
+  }
+  fence_proxy_async();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   grid_dep_wait(); // the setup above may overlap the backward pass; its outputs are read below
   const uint32_t tmem = s.tmem;
-  unsigned char *R = s.region;
   const uint32_t base = smem_u32(R);
-  uint32_t phase = 0;
   bool failed = false;
-  const uint4 one_first = make_uint4(0x3F80u, 0u, 0u, 0u); // BF16 1.0 in the chunk's first value
+  volatile int *abort_flag = &s.abort;
 
-  // One UMMA chain over the tile's 128 rows: D[col] += A^T-tile x B^T-tile, 8 K = 16 steps.
-  auto chain = [&](uint32_t a_off, uint32_t b_off, int nb, uint32_t col, bool first) {
-    const uint32_t a_lbo = (kHid / 8) * 128u, b_lbo = (uint32_t)(nb / 8) * 128u;
-    for (int kk = 0; kk < kWgTile / 16; ++kk)
-      umma_bf16(tmem + col, umma_desc(base + a_off + kk * 2 * a_lbo, a_lbo, 128u),
-                umma_desc(base + b_off + kk * 2 * b_lbo, b_lbo, 128u), wg_idesc(nb), (first && kk == 0) ? 0u : 1u);
-  };
-  // A phase's tiles are complete in shared memory: one thread issues its UMMAs and commits them.
-  auto issue = [&](bool phase_a, bool first) {
-    fence_proxy_async();
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
-      tc_fence_after();
-      if (phase_a) {
-        chain(kWgA3, kWgB3, kWgN3, kWgCol3, first);
-        chain(kWgA2, kWgB2, kWgN3, kWgCol2, first);
-      } else {
-        chain(kWgA1, kWgB1, kWgN1, kWgCol1, first);
-        chain(kWgA4, kWgB4, kWgN4, kWgCol4, first);
-      }
-      umma_commit(&s.bar);
-    }
-  };
-  // The phase's UMMAs have read the region (bounded wait), so it may be rewritten.
-  auto wait = [&]() {
-    if (!mbar_wait_bounded(&s.bar, phase)) failed = true;
-    phase ^= 1u;
-    tc_fence_after();
-  };
-
-  // Phase A's loads for a tile (all 32 16-byte loads in flight at once), then per tile: store A,
-  // issue A's UMMAs, load phase B while they run, store B once they are done, issue B's UMMAs,
-  // load the next tile's phase A while those run.
-  uint4 ad3[8], az2[8], ad2[8], az1[8];
-  auto load_a = [&](int tile) {
-    const long long row = (long long)tile * kWgTile + r;
-    wg_load_half(a.dZ3, row, h, ad3);
-    wg_load_half(a.Z2, row, h, az2);
-    wg_load_half(a.dZ2, row, h, ad2);
-    wg_load_half(a.Z1, row, h, az1);
-  };
-  // The next tile's rows are prefetched into L2 while this one is staged and multiplied.
-  auto prefetch = [&](int tile) {
-    constexpr uint32_t kZ = kWgTile * kHid * 2, kX = kWgTile * kFeat * 2;
-    for (const __nv_bfloat16 *z : {a.dZ3, a.Z2, a.dZ2, a.Z1, a.dZ1, a.Z3})
-      prefetch_l2(reinterpret_cast<const unsigned char *>(z) + (long long)tile * kZ, kZ);
-    prefetch_l2(reinterpret_cast<const unsigned char *>(a.X) + (long long)tile * kX, kX);
-    prefetch_l2(a.dy + (long long)tile * kWgTile, kWgTile * 4);
-    prefetch_l2(a.row_type + (long long)tile * kWgTile, kWgTile * 4);
-  };
-  if (t0 < t1) load_a(t0);
-  for (int tile = t0; tile < t1; ++tile) {
-    const long long row = (long long)tile * kWgTile + r;
-    const bool valid = row < a.rows;
-    const bool first = tile == t0;
-    if (tid == 0 && tile + 1 < t1) prefetch(tile + 1);
-    // Phase A: layers 3 and 2.
-    wg_store_half(R + kWgA3, kHid, h, r, ad3, false);
-    wg_store_half(R + kWgB3, kWgN3, h, r, az2, true);
-    wg_store_half(R + kWgA2, kHid, h, r, ad2, false);
-    wg_store_half(R + kWgB2, kWgN3, h, r, az1, true);
-    {
-      // The bias column (a one per valid row) and 15 zero columns of both B tiles.
-      const uint4 ones = (h == 0 && valid) ? one_first : make_uint4(0, 0, 0, 0);
-      wg_put(R + kWgB3, kWgN3, kHid + h * 8, r, ones);
-      wg_put(R + kWgB2, kWgN3, kHid + h * 8, r, ones);
-    }
-    issue(true, first);
-    // Phase B's loads while phase A's UMMAs run.
-    uint4 bd1[8], bz3[8], bx[4] = {};
-    int type = -1;
-    float d = 0.f;
-    wg_load_half(a.dZ1, row, h, bd1);
-    wg_load_half(a.Z3, row, h, bz3);
-    if (valid) {
-      if (h == 0) {
-        const unsigned char *xt = reinterpret_cast<const unsigned char *>(a.X) + tiled_offset(row, 0, kFeat);
+  // Thread 0 of warp 9 (the loader): one slot's copies of a tile, each 32 KB array tile as
+  // kWgCopies bulk copies.
+  auto load = [&](int j, int tile) {
+    const long long off = (long long)tile * kWgZ;
+    uint64_t *bar = &s.full[j];
+    auto copy = [&](uint32_t dst, const __nv_bfloat16 *p) {
+      const unsigned char *src = reinterpret_cast<const unsigned char *>(p) + off;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) bx[q] = __ldg(reinterpret_cast<const uint4 *>(xt + kmajor_offset(0, q * 8, kFeat)));
-        d = a.dy[row];
-      } else {
-        type = a.row_type[row];
-      }
-    }
-    wait();
-    if (__syncthreads_or(failed)) break;
-    // Phase B: layer 1 (with the one-hot types and the bias column) and the output weights.
-    wg_store_half(R + kWgA1, kHid, h, r, bd1, false);
-    wg_store_half(R + kWgA4, kHid, h, r, bz3, true);
-    if (h == 0) {
-      // X (32 features), the bias column chunk, and dy as two BF16 parts
-#pragma unroll
-      for (int q = 0; q < 4; ++q) wg_put(R + kWgB1, kWgN1, q * 8, r, bx[q]);
-      wg_put(R + kWgB1, kWgN1, kFeat + kMaxTypes, r, valid ? one_first : make_uint4(0, 0, 0, 0));
-      const __nv_bfloat16 hi = __float2bfloat16_rn(d);
-      const __nv_bfloat16 lo = __float2bfloat16_rn(d - __bfloat162float(hi));
-      const uint32_t db = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
-      wg_put(R + kWgB4, kWgN4, 0, r, make_uint4(db, 0u, 0u, 0u));
+      for (int q = 0; q < kWgCopies; ++q)
+        bulk_g2s(R + dst + q * (kWgZ / kWgCopies), src + q * (kWgZ / kWgCopies), kWgZ / kWgCopies, bar);
+    };
+    if (j == 0) {
+      mbar_arrive_expect_tx(bar, 2 * kWgZ);
+      copy(kWgSlot3, a.dZ3);
+      copy(kWgSlot3 + kWgZ, a.Z2);
+    } else if (j == 1) {
+      mbar_arrive_expect_tx(bar, 2 * kWgZ);
+      copy(kWgSlot2, a.dZ2);
+      copy(kWgSlot2 + kWgZ, a.Z1);
+    } else if (j == 2) {
+      mbar_arrive_expect_tx(bar, kWgZ);
+      copy(kWgSlot1, a.dZ1);
     } else {
-      // one-hot of the row's type (8 chunks) and the zero chunks
-#pragma unroll
-      for (int q = 0; q < kMaxTypes / 8; ++q) {
-        uint4 c = make_uint4(0, 0, 0, 0);
-        if (type >= q * 8 && type < q * 8 + 8) {
-          uint32_t *w = reinterpret_cast<uint32_t *>(&c);
-          w[(type - q * 8) >> 1] = ((type - q * 8) & 1) ? 0x3F800000u : 0x3F80u;
-        }
-        wg_put(R + kWgB1, kWgN1, kFeat + q * 8, r, c);
-      }
-      wg_put(R + kWgB1, kWgN1, kFeat + kMaxTypes + 8, r, make_uint4(0, 0, 0, 0));
-      wg_put(R + kWgB4, kWgN4, 8, r, make_uint4(0, 0, 0, 0));
+      mbar_arrive_expect_tx(bar, kWgZ);
+      copy(kWgSlot4, a.Z3);
     }
-    issue(false, first);
-    if (tile + 1 < t1) load_a(tile + 1);
-    wait();
-    if (__syncthreads_or(failed)) break;
+  };
+
+  if (loader) {
+    // Refill each slot with its next tile as soon as the slot's UMMAs have completed.
+    uint32_t eph = 0, issued = 0; // bit j: parity of slot j's next "empty" phase; loads per slot (mod 2)
+    for (int j = 0; j < kWgChains && t0 < t1; ++j) {
+      load(j, t0);
+      issued ^= 1u << j;
+    }
+    for (int tile = t0; tile < t1 && !failed; ++tile) {
+      for (int j = 0; j < kWgChains; ++j) {
+        if (!mbar_wait_bounded(&s.empty[j], (eph >> j) & 1u) || *abort_flag) {
+          failed = true;
+          break;
+        }
+        eph ^= 1u << j;
+        if (tile + 1 < t1) {
+          load(j, tile + 1);
+          issued ^= 1u << j;
+        }
+      }
+    }
+    if (failed) *abort_flag = 1;
+    // After a failure: the copies still in flight land before the block leaves its shared memory
+    // (the phase of each slot's last copy: bounded waits).
+    for (int j = 0; j < kWgChains && failed; ++j)
+      (void)mbar_wait_bounded(&s.full[j], ((issued >> j) & 1u) ^ 1u);
+  } else if (issuer) {
+    // Thread 0 of warp 8: each slot's UMMAs once the workers have built its operands.
+    auto chain = [&](uint32_t a_off, int na, uint32_t b_off, int nb, uint32_t col, bool first) {
+      const uint32_t a_lbo = (uint32_t)(na / 8) * 128u, b_lbo = (uint32_t)(nb / 8) * 128u;
+      for (int kk = 0; kk < kWgTile / 16; ++kk)
+        umma_bf16(tmem + col, umma_desc(base + a_off + kk * 2 * a_lbo, a_lbo, 128u),
+                  umma_desc(base + b_off + kk * 2 * b_lbo, b_lbo, 128u), wg_idesc(nb), (first && kk == 0) ? 0u : 1u);
+    };
+    uint32_t rph = 0; // bit j: parity of slot j's next "ready" phase
+    for (int tile = t0; tile < t1 && !failed; ++tile) {
+      const bool first = tile == t0;
+      for (int j = 0; j < kWgChains; ++j) {
+        if (!mbar_wait_bounded(&s.ready[j], (rph >> j) & 1u) || *abort_flag) {
+          failed = true;
+          *abort_flag = 1;
+          break;
+        }
+        rph ^= 1u << j;
+        tc_fence_after();
+        if (j == 0) {
+          chain(kWgSlot3, kHid, kWgSlot3 + kWgZ, kHid, kWgCol3, first);
+          chain(kWgSlot3, kHid, kWgOnes, kWgNb, kWgColB3, first);
+        } else if (j == 1) {
+          chain(kWgSlot2, kHid, kWgSlot2 + kWgZ, kHid, kWgCol2, first);
+          chain(kWgSlot2, kHid, kWgOnes, kWgNb, kWgColB2, first);
+        } else if (j == 2) {
+          chain(kWgSlot1, kHid, kWgSlot1 + kWgZ, kWgN1, kWgCol1, first);
+          chain(kWgSlot1, kHid, kWgOnes, kWgNb, kWgColB1, first);
+        } else {
+          chain(kWgSlot4, kHid, kWgSlot4 + kWgZ, kWgNb, kWgCol4, first);
+        }
+        umma_commit(&s.empty[j]);
+      }
+    }
+  } else if (worker) {
+    uint32_t fph = 0; // bit j: parity of slot j's next "full" phase
+    for (int tile = t0; tile < t1 && !failed; ++tile) {
+      const long long row = (long long)tile * kWgTile + r;
+      const bool valid = row < a.rows;
+      // The thread-built operands' inputs, in flight while chains 3 and 2 run.
+      uint4 bx[4] = {};
+      int type = -1;
+      float d = 0.f;
+      if (valid) {
+        if (h == 0) {
+          const unsigned char *xt = reinterpret_cast<const unsigned char *>(a.X) + tiled_offset(row, 0, kFeat);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) bx[q] = __ldg(reinterpret_cast<const uint4 *>(xt + kmajor_offset(0, q * 8, kFeat)));
+          d = a.dy[row];
+        } else {
+          type = a.row_type[row];
+        }
+      }
+      for (int j = 0; j < kWgChains; ++j) {
+        if (!mbar_wait_sleep_bounded(&s.full[j], (fph >> j) & 1u) || *abort_flag) {
+          failed = true;
+          *abort_flag = 1;
+          break;
+        }
+        fph ^= 1u << j;
+        if (j == 0) {
+          wg_act_tile(R + kWgSlot3 + kWgZ); // H2
+        } else if (j == 1) {
+          wg_act_tile(R + kWgSlot2 + kWgZ); // H1
+        } else if (j == 2) {
+          // B1 = X | one-hot of the type (rows past the end: zero)
+          unsigned char *b1 = R + kWgSlot1 + kWgZ;
+          if (h == 0) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) wg_put(b1, kWgN1, q * 8, r, bx[q]);
+          } else {
+            const int rel = type & 7, word = rel >> 1;
+            const uint32_t one = (rel & 1) ? 0x3F800000u : 0x3F80u;
+#pragma unroll
+            for (int q = 0; q < kMaxTypes / 8; ++q) {
+              const bool here = (type >> 3) == q && type >= 0;
+              wg_put(b1, kWgN1, kFeat + q * 8, r,
+                     make_uint4(here && word == 0 ? one : 0u, here && word == 1 ? one : 0u,
+                                here && word == 2 ? one : 0u, here && word == 3 ? one : 0u));
+            }
+          }
+        } else {
+          wg_act_tile(R + kWgSlot4); // H3
+          // B4 = dy as two BF16 parts (rows past the end: zero)
+          unsigned char *b4 = R + kWgSlot4 + kWgZ;
+          if (h == 0) {
+            const __nv_bfloat16 hi = __float2bfloat16_rn(d);
+            const __nv_bfloat16 lo = __float2bfloat16_rn(d - __bfloat162float(hi));
+            const uint32_t db = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
+            wg_put(b4, kWgNb, 0, r, make_uint4(db, 0u, 0u, 0u));
+          } else {
+            wg_put(b4, kWgNb, 8, r, make_uint4(0u, 0u, 0u, 0u));
+          }
+        }
+        fence_proxy_async(); // these generic-proxy writes before the UMMAs' reads
+        mbar_arrive(&s.ready[j]);
+      }
+    }
   }
+  tc_fence_before();
+  failed = __syncthreads_or(failed);
+  tc_fence_after();
 
   if (failed) {
     if (tid == 0) atomicOr(a.err, 1u);
-  } else if (t0 < t1) {
+  } else if (worker && t0 < t1) {
     // Accumulators -> this block's partial sums.  Warp w reads TMEM lanes 32 (w % 4) .. + 31 (the
     // M rows: out-features, or H3 features for dw4), warps 0-3 the first half of the columns.
     const int w = tid / 32, lane = tid % 32, m = (w % 4) * 32 + lane;
@@ -273,22 +326,24 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const WgTcArgs 
       for (int j = 0; j < 16; ++j) {
         const int col = c + j;
         const float x = __uint_as_float(v[j]);
-        if (col < kWgCol2) { // dW3 | db3
-          if (col < kHid) p[kWgOffW3 + m * kHid + col] = x;
-          else if (col == kHid) p[kWgOffB3 + m] = x;
-        } else if (col < kWgCol1) { // dW2 | db2
-          const int cc = col - kWgCol2;
-          if (cc < kHid) p[kWgOffW2 + m * kHid + cc] = x;
-          else if (cc == kHid) p[kWgOffB2 + m] = x;
-        } else if (col < kWgCol4) { // dW1 | S | db1
+        if (col < kWgCol2) {
+          p[kWgOffW3 + m * kHid + col] = x;
+        } else if (col < kWgCol1) {
+          p[kWgOffW2 + m * kHid + (col - kWgCol2)] = x;
+        } else if (col < kWgCol4) { // dW1 | S
           const int cc = col - kWgCol1;
           if (cc < kFeat) p[kWgOffW1 + m * kFeat + cc] = x;
-          else if (cc < kFeat + kMaxTypes) p[kWgOffS + m * kMaxTypes + (cc - kFeat)] = x;
-          else if (cc == kFeat + kMaxTypes) p[kWgOffB1 + m] = x;
+          else p[kWgOffS + m * kMaxTypes + (cc - kFeat)] = x;
         } else if (col == kWgCol4) { // dw4: the hi part's column, then the lo part's
           p[kWgOffW4 + m] = x;
         } else if (col == kWgCol4 + 1) {
           p[kWgOffW4 + m] += x;
+        } else if (col == kWgColB3) {
+          p[kWgOffB3 + m] = x;
+        } else if (col == kWgColB2) {
+          p[kWgOffB2 + m] = x;
+        } else if (col == kWgColB1) {
+          p[kWgOffB1 + m] = x;
         }
       }
     }
