@@ -697,9 +697,16 @@ def run_screen(args, dist: Dist):
     rows = sum(len(l) * p.shape[1] for l, p in zip(screen.ligands, screen.poses))
     sur_ms = float(np.mean([st["surrogate_ms"] for st in stats]))
     achieved = rows * MLP_FLOP_PER_ROW / (sur_ms * 1e-3) / 1e12
-    peak = float(peaks.get("bf16_tflops", 1900.8))
+    # The scorer runs inside the screening step (back-to-back steps of tens of ms, the exact
+    # rescoring beside it): the sustained tensor peak is its denominator; the burst one is shown too.
+    burst = float(peaks.get("bf16_tflops", 1900.8))
+    peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
     out["roofline"] = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
-                       "frac": round(achieved / peak, 4), "kernel": "score_tc_kernel",
+                       "frac": round(achieved / peak, 4), "frac_of_burst": round(achieved / burst, 4),
+                       "peak_source": ("MEASURED_PEAKS.json bf16_tflops_sustained (cuBLAS, seconds under the power "
+                                       "cap): the scorer is timed inside the screening step"
+                                       if "bf16_tflops_sustained" in peaks else "fallback 1.7 PFLOP/s sustained"),
+                       "kernel": "score_tc_kernel",
                        "work": f"{MLP_FLOP_PER_ROW} FLOP per (pose, ligand atom) row",
                        "share_of_step": round(sur_ms / step, 3),
                        "traffic": traffic_per_launch(screen.total_poses, "score_tc_kernel")}

@@ -461,24 +461,28 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
     le = launch_chained(wgrad_tc_kernel, (unsigned)wg_grid, (unsigned)(kWgThreads + 64), sizeof(WgTcSmem), c.stream,
                         w);
   ReduceSegs red{};
-  auto reduce = [&](const float *part, int nparts, long long n, long long stride, float *dst) {
+  // Matrix segments come column by column from the gradient kernel (wgrad_tc.cuh) and go back
+  // row-major ([out][in]) into the gradient vector.
+  auto reduce = [&](const float *part, int nparts, long long n, long long stride, float *dst, int tr_cols = 0) {
     const int k = red.nseg++;
     red.part[k] = part;
     red.dst[k] = dst;
     red.stride[k] = stride;
     red.n[k] = (int)n;
     red.nparts[k] = nparts;
+    red.tr_rows[k] = tr_cols > 0 ? kHid : 0;
+    red.tr_cols[k] = tr_cols;
     red.first[k + 1] = red.first[k] + (int)n;
   };
   const float *part = s.part_w.as<float>();
-  reduce(part + kWgOffW3, wg_grid, kHid * kHid, kWgPart, gr + kOffW3);
+  reduce(part + kWgOffW3, wg_grid, kHid * kHid, kWgPart, gr + kOffW3, kHid);
   reduce(part + kWgOffB3, wg_grid, kHid, kWgPart, gr + kOffB3);
-  reduce(part + kWgOffW2, wg_grid, kHid * kHid, kWgPart, gr + kOffW2);
+  reduce(part + kWgOffW2, wg_grid, kHid * kHid, kWgPart, gr + kOffW2, kHid);
   reduce(part + kWgOffB2, wg_grid, kHid, kWgPart, gr + kOffB2);
-  reduce(part + kWgOffW1, wg_grid, kHid * kFeat, kWgPart, gr + kOffW1);
+  reduce(part + kWgOffW1, wg_grid, kHid * kFeat, kWgPart, gr + kOffW1, kFeat);
   reduce(part + kWgOffB1, wg_grid, kHid, kWgPart, gr + kOffB1);
   reduce(part + kWgOffW4, wg_grid, kHid, kWgPart, gr + kOffW4);
-  reduce(part + kWgOffS, wg_grid, kHid * kMaxTypes, kWgPart, s.S_sum.as<float>());
+  reduce(part + kWgOffS, wg_grid, kHid * kMaxTypes, kWgPart, s.S_sum.as<float>(), kMaxTypes);
   reduce(s.dsum.as<float>(), (nb + kLossPoses - 1) / kLossPoses, 1, 1, gr + kOffB4);
   if (le == cudaSuccess)
     le = launch_chained(reduce_segments_kernel, (unsigned)((red.first[red.nseg] + 31) / 32), 32u * kReduceWarps, 0,

@@ -463,6 +463,8 @@ struct ReduceSegs {
   int n[kMaxReduceSegs];
   int nparts[kMaxReduceSegs];
   int first[kMaxReduceSegs + 1]; // prefix sums of n: element e belongs to segment k with first[k] <= e
+  int tr_rows[kMaxReduceSegs];   // > 0: the parts hold a tr_rows x tr_cols matrix column by column
+  int tr_cols[kMaxReduceSegs];   // (element i at (i % tr_rows) * tr_cols + i / tr_rows of dst)
   int nseg;
 };
 
@@ -493,7 +495,8 @@ __global__ void __launch_bounds__(32 * kReduceWarps) reduce_segments_kernel(cons
   if (j == 0 && live) {
     float t = sums[0][lane];
     for (int w = 1; w < kReduceWarps; ++w) t += sums[w][lane];
-    r.dst[k][e - r.first[k]] = t;
+    const int i = e - r.first[k], R = r.tr_rows[k];
+    r.dst[k][R > 0 ? (i % R) * r.tr_cols[k] + i / R : i] = t;
   }
 }
 

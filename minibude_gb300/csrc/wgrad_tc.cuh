@@ -43,7 +43,9 @@ constexpr int kWgNb = 16;                // N of the output-weight and bias chai
 constexpr int kWgCol3 = 0, kWgCol2 = kHid, kWgCol1 = 2 * kHid, kWgCol4 = kWgCol1 + kWgN1,
               kWgColB3 = kWgCol4 + kWgNb, kWgColB2 = kWgColB3 + kWgNb, kWgColB1 = kWgColB2 + kWgNb;
 constexpr int kWgCols = kWgColB1 + kWgNb; // 416 TMEM columns used of the 512 allocated
-// Partial sums per block, floats: [dW3 128x128 | db3 128 | dW2 | db2 | dW1 128x32 | S 128x64 | db1 | dw4]
+// Partial sums per block, floats: [dW3 | db3 128 | dW2 | db2 | dW1 | S | db1 | dw4], the matrices
+// column by column (element [out][in] at in * 128 + out: a warp's 32 lanes, 32 consecutive out
+// rows of one TMEM column, store 128 contiguous bytes); the reduction writes them back row-major.
 constexpr int kWgOffW3 = 0, kWgOffB3 = kWgOffW3 + kHid * kHid, kWgOffW2 = kWgOffB3 + kHid,
               kWgOffB2 = kWgOffW2 + kHid * kHid, kWgOffW1 = kWgOffB2 + kHid, kWgOffS = kWgOffW1 + kHid * kFeat,
               kWgOffB1 = kWgOffS + kHid * kMaxTypes, kWgOffW4 = kWgOffB1 + kHid, kWgPart = kWgOffW4 + kHid;
@@ -87,22 +89,37 @@ struct WgTcArgs {
   unsigned int *err;                     // bit 0: a bounded wait ran out
 };
 
-// 8 BF16 values as a 16-byte chunk of one row into an MN-major tile (features f0..f0+7 of row k).
-__device__ __forceinline__ void wg_put(unsigned char *tile, int nmn, int f0, int k, uint4 v) {
-  *reinterpret_cast<uint4 *>(tile + mnmajor_offset(f0, k, nmn)) = v;
+// 16-byte shared-memory load and store by shared-window address (ld/st.shared: the accesses
+// stay on the shared-memory path instead of the generic load/store queue).
+__device__ __forceinline__ uint4 lds128(uint32_t addr) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ void sts128(uint32_t addr, uint4 v) {
+  asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
 }
 
-// H = act(Z) in place over one 32 KB tile: 2,048 16-byte chunks, 8 per thread.
-__device__ __forceinline__ void wg_act_tile(unsigned char *tile) {
+// 8 BF16 values as a 16-byte chunk of one row into an MN-major tile (features f0..f0+7 of row k);
+// `tile` is a shared-window address.
+__device__ __forceinline__ void wg_put(uint32_t tile, int nmn, int f0, int k, uint4 v) {
+  sts128(tile + mnmajor_offset(f0, k, nmn), v);
+}
+
+// H = act(Z) in place over one 32 KB tile at shared-window address `tile`: 2,048 16-byte chunks,
+// 8 per worker thread, all 8 loads in flight before the first store.
+__device__ __forceinline__ void wg_act_tile(uint32_t tile) {
+  uint4 v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = lds128(tile + (uint32_t)(threadIdx.x + i * kWgThreads) * 16u);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    uint4 *c = reinterpret_cast<uint4 *>(tile) + threadIdx.x + i * kWgThreads;
-    uint4 v = *c;
-    v.x = act_bf16x2(v.x);
-    v.y = act_bf16x2(v.y);
-    v.z = act_bf16x2(v.z);
-    v.w = act_bf16x2(v.w);
-    *c = v;
+    v[i].x = act_bf16x2(v[i].x);
+    v[i].y = act_bf16x2(v[i].y);
+    v[i].z = act_bf16x2(v[i].z);
+    v[i].w = act_bf16x2(v[i].w);
+    sts128(tile + (uint32_t)(threadIdx.x + i * kWgThreads) * 16u, v[i]);
   }
 }
 
@@ -136,7 +153,7 @@ __global__ void __launch_bounds__(kWgThreads + 64, 1) wgrad_tc_kernel(const WgTc
   if (worker) {
     // The tile of ones for the bias chains: B[n][k] = 1 for n = 0, 0 for n = 1..15.
     const uint4 one_first = make_uint4(0x3F80u, 0u, 0u, 0u), zero = make_uint4(0u, 0u, 0u, 0u);
-    wg_put(R + kWgOnes, kWgNb, h * 8, r, h == 0 ? one_first : zero);
+    wg_put(smem_u32(R) + kWgOnes, kWgNb, h * 8, r, h == 0 ? one_first : zero);
   }
   fence_proxy_async();
   tc_fence_before();
@@ -262,12 +279,12 @@ __global__ void __launch_bounds__(kWgThreads + 64, 1) wgrad_tc_kernel(const WgTc
         }
         fph ^= 1u << j;
         if (j == 0) {
-          wg_act_tile(R + kWgSlot3 + kWgZ); // H2
+          wg_act_tile(base + kWgSlot3 + kWgZ); // H2
         } else if (j == 1) {
-          wg_act_tile(R + kWgSlot2 + kWgZ); // H1
+          wg_act_tile(base + kWgSlot2 + kWgZ); // H1
         } else if (j == 2) {
           // B1 = X | one-hot of the type (rows past the end: zero)
-          unsigned char *b1 = R + kWgSlot1 + kWgZ;
+          const uint32_t b1 = base + kWgSlot1 + kWgZ;
           if (h == 0) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) wg_put(b1, kWgN1, q * 8, r, bx[q]);
@@ -283,9 +300,9 @@ __global__ void __launch_bounds__(kWgThreads + 64, 1) wgrad_tc_kernel(const WgTc
             }
           }
         } else {
-          wg_act_tile(R + kWgSlot4); // H3
+          wg_act_tile(base + kWgSlot4); // H3
           // B4 = dy as two BF16 parts (rows past the end: zero)
-          unsigned char *b4 = R + kWgSlot4 + kWgZ;
+          const uint32_t b4 = base + kWgSlot4 + kWgZ;
           if (h == 0) {
             const __nv_bfloat16 hi = __float2bfloat16_rn(d);
             const __nv_bfloat16 lo = __float2bfloat16_rn(d - __bfloat162float(hi));
@@ -327,13 +344,13 @@ __global__ void __launch_bounds__(kWgThreads + 64, 1) wgrad_tc_kernel(const WgTc
         const int col = c + j;
         const float x = __uint_as_float(v[j]);
         if (col < kWgCol2) {
-          p[kWgOffW3 + m * kHid + col] = x;
+          p[kWgOffW3 + col * kHid + m] = x;
         } else if (col < kWgCol1) {
-          p[kWgOffW2 + m * kHid + (col - kWgCol2)] = x;
+          p[kWgOffW2 + (col - kWgCol2) * kHid + m] = x;
         } else if (col < kWgCol4) { // dW1 | S
           const int cc = col - kWgCol1;
-          if (cc < kFeat) p[kWgOffW1 + m * kFeat + cc] = x;
-          else p[kWgOffS + m * kMaxTypes + (cc - kFeat)] = x;
+          if (cc < kFeat) p[kWgOffW1 + cc * kHid + m] = x;
+          else p[kWgOffS + (cc - kFeat) * kHid + m] = x;
         } else if (col == kWgCol4) { // dw4: the hi part's column, then the lo part's
           p[kWgOffW4 + m] = x;
         } else if (col == kWgCol4 + 1) {
