@@ -20,14 +20,19 @@
 // TMA bulk copies, without registers.  Shared memory holds one slot per chain (224 KB in all):
 //   slot 3: dZ3 | Z2 -> H2     slot 2: dZ2 | Z1 -> H1     slot 1: dZ1 | X, T (built by threads)
 //   slot 4: Z3 -> H3 | dy (built by threads)               and the constant tile of ones.
-// Per tile the block runs the chains in the order 3, 2, 1, 4: wait for the slot's copies, rebuild
-// H in place (act) or write the thread-built operand, then one thread issues the chain's UMMAs and
-// commits them to the slot's "empty" barrier, and refills the slot of the chain before (whose UMMAs
-// were committed one chain earlier) with its next tile.  Every slot's next copies are therefore in
-// flight for three chains' time, about three quarters of a tile.  All waits are bounded.
+// The block is warp-specialised, three roles meeting on three barriers per slot:
+//   * eight worker warps take the chains of each tile in the order 3, 2, 1, 4: wait for the
+//     slot's copies ("full"), rebuild H in place (act) or write the thread-built operand, and
+//     arrive on the slot's "ready" barrier;
+//   * the issuer (thread 0 of warp 8) waits for "ready", issues the chain's UMMAs and commits them
+//     to the slot's "empty" barrier;
+//   * the loader (thread 0 of warp 9) waits for "empty" and refills the slot with its next tile.
+// Every wait is bounded; one that runs out raises a shared abort flag and every role leaves.
 //
 // A block owns a contiguous range of 128-row tiles (the same on every run), so the partial sums
-// and their fixed-order reduction over blocks (reduce_segments_kernel) are deterministic.
+// and their fixed-order reduction over blocks (reduce_segments_kernel) are deterministic.  The
+// partial sums are stored column by column (coalesced), and the reduction writes each matrix back
+// row-major.
 #pragma once
 #include <cstdint>
 
@@ -37,7 +42,7 @@
 namespace bude {
 
 constexpr int kWgTile = 128;    // rows per tile: K of 8 UMMAs
-constexpr int kWgThreads = 256; // two threads per row for the thread-built operands
+constexpr int kWgThreads = 256; // worker threads: two per row for the thread-built operands
 constexpr int kWgN1 = kFeat + kMaxTypes; // N of the layer-1 chain (X | one-hot)
 constexpr int kWgNb = 16;                // N of the output-weight and bias chains
 constexpr int kWgCol3 = 0, kWgCol2 = kHid, kWgCol1 = 2 * kHid, kWgCol4 = kWgCol1 + kWgN1,
