@@ -159,11 +159,4 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 // kernel made the training step slower, 6.77 s against 6.03 s for 80 epochs.)
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
-// Bulk prefetch of `bytes` of global memory into L2 (no registers, no completion to wait for), so
-// that the loads which follow later hit L2 instead of waiting on HBM.  src 16-byte aligned, bytes a
-// multiple of 16, the range inside one allocation.
-__device__ __forceinline__ void prefetch_l2(const void *src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
-}
-
 } // namespace bude

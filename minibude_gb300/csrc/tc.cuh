@@ -157,11 +157,6 @@ template <class F> __device__ __forceinline__ void tmem_rows128(uint32_t taddr, 
   }
 }
 
-// 2 consecutive FP32 columns of this thread's TMEM lane.
-__device__ __forceinline__ void tmem_ld2(uint32_t taddr, uint32_t (&v)[2]) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(v[0]), "=r"(v[1]) : "r"(taddr) : "memory");
-}
-
 // Named barrier over `nthreads` threads (a multiple of 32); id 0 is __syncthreads' barrier.
 __device__ __forceinline__ void named_sync(uint32_t id, uint32_t nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
