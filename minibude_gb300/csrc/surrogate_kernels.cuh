@@ -36,6 +36,7 @@
 
 #include <cstdint>
 
+#include "../../include/minibude_gb300.h"
 #include "mlp.cuh"
 #include "ptx.cuh"
 #include "tc.cuh"
@@ -468,6 +469,12 @@ struct ReduceSegs {
   int nseg;
 };
 
+// Destination of element i of a segment whose parts hold an R x C matrix column by column (element
+// [row][col] at col * R + row) in the row-major result; R = 0: the identity.
+__host__ __device__ __forceinline__ int reduce_dst_index(int i, int R, int C) {
+  return R > 0 ? (i % R) * C + i / R : i;
+}
+
 __global__ void __launch_bounds__(32 * kReduceWarps) reduce_segments_kernel(const ReduceSegs r) {
   grid_dep_wait();
   __shared__ float sums[kReduceWarps][32];
@@ -495,8 +502,7 @@ __global__ void __launch_bounds__(32 * kReduceWarps) reduce_segments_kernel(cons
   if (j == 0 && live) {
     float t = sums[0][lane];
     for (int w = 1; w < kReduceWarps; ++w) t += sums[w][lane];
-    const int i = e - r.first[k], R = r.tr_rows[k];
-    r.dst[k][R > 0 ? (i % R) * r.tr_cols[k] + i / R : i] = t;
+    r.dst[k][reduce_dst_index(e - r.first[k], r.tr_rows[k], r.tr_cols[k])] = t;
   }
 }
 
