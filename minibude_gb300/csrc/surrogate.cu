@@ -54,7 +54,7 @@ struct Surrogate {
   long long step = 0;
   // training scratch
   DevBuf X, row_type, Z1, Z2, Z3, dZ1, dZ2, dZ3, y, dy, pred, loss, dsum, part_w, S_sum;
-  DevBuf labels, pose_lig_first, pose_lig_n, epoch_pose, epoch_rowoff;
+  DevBuf labels, pose_lig_first, pose_lig_n, epoch_pose, epoch_rowoff, epoch_pose2, epoch_rowoff2, epoch_loss;
   long long rows_cap = 0;
   // scoring
   DevBuf items, scores, next;
@@ -86,7 +86,8 @@ void release_surrogate(Context &c) {
                    &s.w1t_bf, &s.w2t_bf, &s.w3t_bf, &s.emb_h, &s.w1_h, &s.w2_h, &s.w3_h, &s.grid, &s.protein4, &s.X, &s.row_type, &s.Z1,
                    &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3, &s.y, &s.dy, &s.pred, &s.loss, &s.dsum,
                    &s.part_w, &s.S_sum, &s.labels, &s.pose_lig_first, &s.pose_lig_n,
-                   &s.epoch_pose, &s.epoch_rowoff, &s.items, &s.scores, &s.next};
+                   &s.epoch_pose, &s.epoch_rowoff, &s.epoch_pose2, &s.epoch_rowoff2, &s.epoch_loss, &s.items,
+                   &s.scores, &s.next};
   for (DevBuf *b : all) b->release();
   delete c.surrogate;
   c.surrogate = nullptr;
@@ -375,9 +376,10 @@ static cudaError_t launch_chained(void (*kernel)(KArgs...), unsigned grid, unsig
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
-// One optimisation step on `nb` poses whose indices/row offsets are at dpose/drowoff.
+// One optimisation step on `nb` poses whose indices/row offsets are at dpose/drowoff; the poses'
+// squared errors go to loss_out (device, nb floats; nullptr: the scratch array s.loss).
 static int train_step(Context &c, Surrogate &s, const int *dpose, const int *drowoff, int nb, long long rows, float lr,
-                      float *loss_sum_dev_host) {
+                      float *loss_out) {
   const float *p = s.params.as<float>();
   float *gr = s.grads.as<float>();
   RowMap m;
@@ -419,7 +421,8 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   if (le == cudaSuccess)
     le = launch_chained(train_loss_kernel, (unsigned)((nb + kLossPoses - 1) / kLossPoses), 32u * kLossPoses, 0,
                         c.stream, m, s.y.as<float>(), p + kOffB4, s.labels.as<float>(), s.pred.as<float>(),
-                        s.loss.as<float>(), s.dy.as<float>(), s.dsum.as<float>(), 1.f / (float)nb);
+                        loss_out ? loss_out : s.loss.as<float>(), s.dy.as<float>(), s.dsum.as<float>(),
+                        1.f / (float)nb);
   {
     // Backward through the hidden layers on the tensor cores (score_tc.cuh): dz3, dz2, dz1 as BF16.
     TrainBwdTcArgs b;
@@ -503,7 +506,6 @@ static int train_step(Context &c, Surrogate &s, const int *dpose, const int *dro
   if (le != cudaSuccess) return cuda_error(le, "surrogate training step launch");
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "surrogate training step");
-  (void)loss_sum_dev_host;
   return BUDE_OK;
 }
 
@@ -579,7 +581,7 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
   cudaError_t e = copy_sync(c, hl.data(), s.labels.ptr, (size_t)np * 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = copy_sync(c, edge.data(), c.b_edge_mask.ptr, edge.size() * 4, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_error(e, "labels read-back");
-  std::vector<int> order, rowoff;
+  std::vector<int> order;
   order.reserve((size_t)np);
   for (int l = 0; l < c.nligands; ++l) {
     if (c.b_lig_all_host[(size_t)l]) continue;
@@ -602,35 +604,61 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
   const int nb_full = (int)std::min<long long>(batch, n_used);
   const int steps_per_epoch = (int)((n_used + nb_full - 1) / nb_full);
   const long long total_steps = (long long)epochs * steps_per_epoch;
+  const size_t nrow_off = (size_t)(n_used + steps_per_epoch);
   std::mt19937_64 rng(seed);
-  rc = s.epoch_pose.reserve((size_t)np * 4, "epoch poses");
-  if (!rc) rc = s.epoch_rowoff.reserve((size_t)(np + steps_per_epoch) * 4, "epoch row offsets");
+  // Epochs are double-buffered: while the GPU runs epoch e from one pair of device arrays (pose
+  // order, row offsets), the host shuffles epoch e + 1 into pinned memory and a copy stream moves
+  // it into the other pair once the kernels of epoch e - 1 have finished with it.  The last
+  // epoch's per-pose losses collect on the device and are read once.
+  DevBuf *dpose[2] = {&s.epoch_pose, &s.epoch_pose2}, *drow[2] = {&s.epoch_rowoff, &s.epoch_rowoff2};
+  for (int k = 0; k < 2 && !rc; ++k) {
+    rc = dpose[k]->reserve((size_t)np * 4, "epoch poses");
+    if (!rc) rc = drow[k]->reserve(nrow_off * 4, "epoch row offsets");
+  }
+  if (!rc) rc = s.epoch_loss.reserve((size_t)n_used * 4, "last-epoch losses");
   if (rc) return rc;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0, c.stream);
-  double last_loss = 0;
-  long long done = 0;
-  for (int ep = 0; ep < epochs && !rc; ++ep) {
+  int *hpose[2] = {}, *hrow[2] = {};
+  cudaStream_t cs = nullptr;
+  cudaEvent_t copied[2] = {}, used[2] = {}, e0 = nullptr, e1 = nullptr;
+  bool setup_ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
+  for (int k = 0; k < 2 && setup_ok; ++k)
+    setup_ok = cudaMallocHost((void **)&hpose[k], (size_t)n_used * 4) == cudaSuccess &&
+               cudaMallocHost((void **)&hrow[k], nrow_off * 4) == cudaSuccess &&
+               cudaEventCreateWithFlags(&copied[k], cudaEventDisableTiming) == cudaSuccess &&
+               cudaEventCreateWithFlags(&used[k], cudaEventDisableTiming) == cudaSuccess;
+  setup_ok = setup_ok && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+  std::vector<long long> rows_of[2] = {std::vector<long long>(steps_per_epoch),
+                                       std::vector<long long>(steps_per_epoch)};
+  // Shuffle epoch `ep` into host buffer k and queue its copy into device pair k.
+  auto prepare = [&](int ep, int k) -> int {
     std::shuffle(order.begin(), order.end(), rng);
     // Row offsets of every batch of the epoch, one block of (batch + 1) entries per step.
-    rowoff.clear();
-    std::vector<long long> rows_of(steps_per_epoch);
+    size_t w = 0;
     for (int st = 0; st < steps_per_epoch; ++st) {
       const long long a = (long long)st * nb_full, b = std::min(n_used, a + nb_full);
       int r = 0;
       for (long long i = a; i < b; ++i) {
-        rowoff.push_back(r);
+        hrow[k][w++] = r;
         r += lig_n[(size_t)order[(size_t)i]];
       }
-      rowoff.push_back(r);
-      rows_of[st] = r;
+      hrow[k][w++] = r;
+      rows_of[k][(size_t)st] = r;
     }
-    cudaMemcpyAsync(s.epoch_pose.ptr, order.data(), (size_t)n_used * 4, cudaMemcpyHostToDevice, c.stream);
-    cudaMemcpyAsync(s.epoch_rowoff.ptr, rowoff.data(), rowoff.size() * 4, cudaMemcpyHostToDevice, c.stream);
-    cudaStreamSynchronize(c.stream); // the host vectors are rewritten next epoch
-    double loss_sum = 0;
+    std::memcpy(hpose[k], order.data(), (size_t)n_used * 4);
+    cudaError_t ce = ep >= 2 ? cudaStreamWaitEvent(cs, used[k], 0) : cudaSuccess;
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(dpose[k]->ptr, hpose[k], (size_t)n_used * 4, cudaMemcpyHostToDevice, cs);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(drow[k]->ptr, hrow[k], w * 4, cudaMemcpyHostToDevice, cs);
+    if (ce == cudaSuccess) ce = cudaEventRecord(copied[k], cs);
+    return ce == cudaSuccess ? BUDE_OK : cuda_error(ce, "epoch order copy");
+  };
+  if (!setup_ok) rc = set_error(BUDE_ERR_CUDA, "training pipeline setup (stream, events, pinned buffers)");
+  if (!rc) cudaEventRecord(e0, c.stream);
+  if (!rc && epochs > 0) rc = prepare(0, 0);
+  long long done = 0;
+  for (int ep = 0; ep < epochs && !rc; ++ep) {
+    const int k = ep & 1;
+    cudaError_t ce = cudaStreamWaitEvent(c.stream, copied[k], 0);
+    if (ce != cudaSuccess) rc = cuda_error(ce, "epoch order wait");
     long long ro = 0;
     for (int st = 0; st < steps_per_epoch && !rc; ++st) {
       const long long a = (long long)st * nb_full, b = std::min(n_used, a + nb_full);
@@ -638,25 +666,47 @@ int surrogate_train(Context &c, int epochs, int batch, float lr, const float *la
       // Cosine decay from lr to lr / 20 over the run.
       const double frac = total_steps > 1 ? (double)done / (double)(total_steps - 1) : 0.0;
       const float lr_now = (float)(lr * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(M_PI * frac))));
-      rc = train_step(c, s, s.epoch_pose.as<int>() + a, s.epoch_rowoff.as<int>() + ro, nb, rows_of[st], lr_now,
-                      nullptr);
+      rc = train_step(c, s, dpose[k]->as<int>() + a, drow[k]->as<int>() + ro, nb, rows_of[k][(size_t)st], lr_now,
+                      ep == epochs - 1 ? s.epoch_loss.as<float>() + a : nullptr);
       ro += nb + 1;
       ++done;
-      if (!rc && ep == epochs - 1) {
-        std::vector<float> lh((size_t)nb);
-        const cudaError_t e = copy_sync(c, lh.data(), s.loss.ptr, (size_t)nb * 4, cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) rc = cuda_error(e, "loss read-back");
-        for (float v : lh) loss_sum += v;
-      }
     }
-    last_loss = loss_sum / (double)n_used;
+    if (!rc) {
+      ce = cudaEventRecord(used[k], c.stream);
+      if (ce != cudaSuccess) rc = cuda_error(ce, "epoch event");
+    }
+    if (!rc && ep + 1 < epochs) {
+      // Host buffer k ^ 1 last fed epoch ep - 1, whose copy finished before that epoch ran.
+      ce = cudaEventSynchronize(copied[k ^ 1]);
+      rc = ce == cudaSuccess ? prepare(ep + 1, k ^ 1) : cuda_error(ce, "epoch order copy");
+    }
   }
-  cudaEventRecord(e1, c.stream);
+  if (e1) cudaEventRecord(e1, c.stream);
   e = cudaStreamSynchronize(c.stream);
   if (!rc && e != cudaSuccess) rc = cuda_error(e, "surrogate training");
+  double last_loss = 0;
+  if (!rc && epochs > 0) {
+    // The last epoch's losses in pose order, summed in that order.
+    std::vector<float> lh((size_t)n_used);
+    e = copy_sync(c, lh.data(), s.epoch_loss.ptr, (size_t)n_used * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_error(e, "loss read-back");
+    double loss_sum = 0;
+    for (float v : lh) loss_sum += v;
+    last_loss = loss_sum / (double)n_used;
+  }
+  if (cs) {
+    cudaStreamSynchronize(cs);
+    cudaStreamDestroy(cs);
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (hpose[k]) cudaFreeHost(hpose[k]);
+    if (hrow[k]) cudaFreeHost(hrow[k]);
+    if (copied[k]) cudaEventDestroy(copied[k]);
+    if (used[k]) cudaEventDestroy(used[k]);
+  }
   if (!rc && train_ms) cudaEventElapsedTime(train_ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
   if (!rc && final_loss) *final_loss = (float)last_loss;
   return rc;
 }
