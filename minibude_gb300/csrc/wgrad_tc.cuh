@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(kWgThreads + 64, 1) wgrad_tc_kernel(const WgTc
         umma_bf16(tmem + col, umma_desc(base + a_off + kk * 2 * a_lbo, a_lbo, 128u),
                   umma_desc(base + b_off + kk * 2 * b_lbo, b_lbo, 128u), wg_idesc(nb), (first && kk == 0) ? 0u : 1u);
     };
-    uint32_t rph = 0; // bit j: parity of slot j's next "ready" phase
+    // Bit j: parity of slot j's next "ready" phase; commits to slot j (mod 2); slot j committed to.
+    uint32_t rph = 0, cph = 0, cmask = 0;
     for (int tile = t0; tile < t1 && !failed; ++tile) {
       const bool first = tile == t0;
       for (int j = 0; j < kWgChains; ++j) {
@@ -255,8 +256,14 @@ __global__ void __launch_bounds__(kWgThreads + 64, 1) wgrad_tc_kernel(const WgTc
           chain(kWgSlot4, kHid, kWgSlot4 + kWgZ, kWgNb, kWgCol4, first);
         }
         umma_commit(&s.empty[j]);
+        cph ^= 1u << j;
+        cmask |= 1u << j;
       }
     }
+    // After a failure the loader may have stopped waiting for "empty": the last UMMAs of every
+    // slot complete before the block releases its TMEM (bounded waits on each slot's last phase).
+    for (int j = 0; j < kWgChains && failed; ++j)
+      if ((cmask >> j) & 1u) (void)mbar_wait_bounded(&s.empty[j], ((cph >> j) & 1u) ^ 1u);
   } else if (worker) {
     uint32_t fph = 0; // bit j: parity of slot j's next "full" phase
     for (int tile = t0; tile < t1 && !failed; ++tile) {
