@@ -43,7 +43,7 @@ struct Surrogate {
   bool ready = false;
   int ntypes = 0;
   DevBuf params, adam_m, adam_v, grads;
-  DevBuf emb_bf, w1_bf, w2_bf, w3_bf, w1t_bf, w2t_bf, w3t_bf;
+  DevBuf emb_bf, w1_bf, w2_bf, w3_bf, w2t_bf, w3t_bf; // w2t, w3t: transposed copies (backward pass)
   DevBuf emb_h, w1_h, w2_h, w3_h; // FP16 copies for the tcgen05 scorer
   float w4_host[kHid] = {};        // host copy of the output weights (scorer launch parameters)
   bool w4_host_valid = false;      // false whenever the weights may have changed
@@ -83,7 +83,7 @@ void release_surrogate(Context &c) {
   Surrogate &s = *c.surrogate;
   release_textures(s);
   DevBuf *all[] = {&s.params, &s.adam_m, &s.adam_v, &s.grads, &s.emb_bf, &s.w1_bf, &s.w2_bf, &s.w3_bf,
-                   &s.w1t_bf, &s.w2t_bf, &s.w3t_bf, &s.emb_h, &s.w1_h, &s.w2_h, &s.w3_h, &s.grid, &s.protein4, &s.X, &s.row_type, &s.Z1,
+                   &s.w2t_bf, &s.w3t_bf, &s.emb_h, &s.w1_h, &s.w2_h, &s.w3_h, &s.grid, &s.protein4, &s.X, &s.row_type, &s.Z1,
                    &s.Z2, &s.Z3, &s.dZ1, &s.dZ2, &s.dZ3, &s.y, &s.dy, &s.pred, &s.loss, &s.dsum,
                    &s.part_w, &s.S_sum, &s.labels, &s.pose_lig_first, &s.pose_lig_n,
                    &s.epoch_pose, &s.epoch_rowoff, &s.epoch_pose2, &s.epoch_rowoff2, &s.epoch_loss, &s.items,
@@ -121,7 +121,7 @@ static BfCopies bf_copies(Surrogate &s) {
     c.half[k] = half ? half->as<__half>() : nullptr;
   };
   add(kOffEmb, kMaxTypes, kEmb, &s.emb_bf, nullptr, &s.emb_h);
-  add(kOffW1, kHid, kFeat, &s.w1_bf, &s.w1t_bf, &s.w1_h);
+  add(kOffW1, kHid, kFeat, &s.w1_bf, nullptr, &s.w1_h);
   add(kOffW2, kHid, kHid, &s.w2_bf, &s.w2t_bf, &s.w2_h);
   add(kOffW3, kHid, kHid, &s.w3_bf, &s.w3t_bf, &s.w3_h);
   return c;
@@ -241,7 +241,6 @@ int surrogate_init(Context &c, const bude_atom *protein, int natpro, const bude_
   if (!rc) rc = s.grads.reserve(pb, "surrogate grads");
   if (!rc) rc = s.emb_bf.reserve(kMaxTypes * kEmb * 2, "emb bf16");
   if (!rc) rc = s.w1_bf.reserve(kHid * kFeat * 2, "w1 bf16");
-  if (!rc) rc = s.w1t_bf.reserve(kHid * kFeat * 2, "w1t bf16");
   if (!rc) rc = s.w2_bf.reserve(kHid * kHid * 2, "w2 bf16");
   if (!rc) rc = s.w2t_bf.reserve(kHid * kHid * 2, "w2t bf16");
   if (!rc) rc = s.w3_bf.reserve(kHid * kHid * 2, "w3 bf16");
