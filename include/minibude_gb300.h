@@ -198,7 +198,8 @@ int bude_surrogate_init(bude_gpu_ctx *ctx, const bude_atom *protein, int32_t nat
  * shuffled batches of `batch_poses` poses with Adam (learning rate `lr`, cosine decay to lr/20).
  * labels (NULL: exact energies computed here with the batched exact kernel) are per pose in batch
  * order.  The loss is the mean squared error on the compressed scale 20*asinh(E/20).  final_loss
- * (optional): mean loss of the last epoch; train_ms (optional): GPU time. */
+ * (optional): mean loss of the last epoch; train_ms (optional): elapsed time of the epochs on the
+ * context's stream (CUDA events from before the first epoch's shuffle to after the last step). */
 int bude_surrogate_train(bude_gpu_ctx *ctx, int32_t epochs, int32_t batch_poses, float lr, const float *labels,
                          uint64_t seed, float *final_loss, float *train_ms);
 
